@@ -1,0 +1,259 @@
+"""numpy front end of the CPU oracle (test infrastructure only).
+
+Every function mirrors one reference operator on the rasteriser path and runs
+the C++ restatement in oracle/ubs_oracle.cpp.  dtype float32 mirrors the
+reference's FP32 kernels; float64 is used for finite-difference checks.
+Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline use this.
+"""
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+import build_oracle  # noqa: E402
+
+_lib = None
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_I64 = ctypes.c_int64
+_U32 = ctypes.c_uint32
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build_oracle.build())
+        for s, ft in (("f32", ctypes.c_float), ("f64", ctypes.c_double)):
+            g = lambda n: getattr(_lib, "ubso_%s_%s" % (n, s))  # noqa: E731
+            g("rotmat_fwd").argtypes = [_I64, _P, _I64, _P]
+            g("rotmat_bwd").argtypes = [_I64, _P, _P]
+            g("covar_fwd").argtypes = [_I64, _I, _P, _P, _P, _P, _P, _I, _I, _P]
+            g("covar_bwd").argtypes = [_I64, _I, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P]
+            g("cond_fwd").argtypes = [_I64, _I, _P, _P, _P, _P, _P, _P, _P, _P]
+            g("cond_bwd").argtypes = [_I64, _I] + [_P] * 12 + [_I]
+            g("project_fwd").argtypes = ([_I, _I64] + [_P] * 6 + [_I, _I, ft, ft, ft, ft]
+                                         + [_P] * 5)
+            g("project_bwd").argtypes = ([_I, _I64] + [_P] * 6 + [_I, _I, ft] + [_P] * 12)
+            g("raster_fwd").argtypes = ([_I, _I64, _I, _I64] + [_P] * 7
+                                        + [_I, _I, _I, _I, _I] + [_P] * 5)
+            g("raster_bwd").argtypes = ([_I, _I64, _I, _I64] + [_P] * 7
+                                        + [_I, _I, _I, _I, _I] + [_P] * 11)
+        _lib.ubso_isect_count.argtypes = [_I, _I64, _P, _P, _U32, _U32, _U32, _P]
+        _lib.ubso_isect_count.restype = _I64
+        _lib.ubso_isect_emit_sort.argtypes = [_I, _I64, _P, _P, _P, _U32, _U32, _U32, _P,
+                                              _I64, _I, _P, _P]
+        _lib.ubso_offset_encode.argtypes = [_I64, _P, _I, _U32, _U32, _P]
+        _lib.ubso_num_threads.restype = _I
+        _lib.ubso_set_threads.argtypes = [_I]
+    return _lib
+
+
+def num_threads():
+    return lib().ubso_num_threads()
+
+
+def set_threads(n):
+    lib().ubso_set_threads(int(n))
+
+
+def _sfx(dtype):
+    return "f64" if np.dtype(dtype) == np.float64 else "f32"
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _fn(name, dtype):
+    return getattr(lib(), "ubso_%s_%s" % (name, _sfx(dtype)))
+
+
+def l_triangle_to_rotmat(l, dtype=np.float32):
+    l = _c(l, dtype)
+    n = l.shape[0]
+    R = np.zeros((n, 3, 3), dtype)
+    _fn("rotmat_fwd", dtype)(n, _p(l), l.shape[1], _p(R))
+    return R
+
+
+def l_triangle_to_rotmat_bwd(v_R, dtype=np.float32):
+    v_R = _c(v_R, dtype)
+    n = v_R.shape[0]
+    out = np.zeros((n, 3), dtype)
+    _fn("rotmat_bwd", dtype)(n, _p(v_R), _p(out))
+    return out
+
+
+def rot_scale_l_triangle_to_covar(rot, scale, l_tri, rest_i, rest_j, spatial_block=False,
+                                  dtype=np.float32):
+    rot, scale, l_tri = _c(rot, dtype), _c(scale, dtype), _c(l_tri, dtype)
+    ri, rj = _c(rest_i, np.int32), _c(rest_j, np.int32)
+    n, D = scale.shape
+    dim = 3 if (spatial_block or D == 3) else D
+    out = np.zeros((n, dim, dim), dtype)
+    _fn("covar_fwd", dtype)(n, D, _p(rot), _p(scale), _p(l_tri), _p(ri), _p(rj), len(ri),
+                            int(spatial_block), _p(out))
+    return out
+
+
+def rot_scale_l_triangle_to_covar_bwd(rot, scale, l_tri, rest_i, rest_j, v_covar,
+                                      spatial_block=False, dtype=np.float32):
+    rot, scale, l_tri = _c(rot, dtype), _c(scale, dtype), _c(l_tri, dtype)
+    ri, rj = _c(rest_i, np.int32), _c(rest_j, np.int32)
+    v_covar = _c(v_covar, dtype)
+    n, D = scale.shape
+    vr = np.zeros((n, 3, 3), dtype)
+    vs = np.zeros((n, D), dtype)
+    vl = np.zeros((n, D * (D - 1) // 2), dtype)
+    _fn("covar_bwd", dtype)(n, D, _p(rot), _p(scale), _p(l_tri), _p(ri), _p(rj), len(ri),
+                            int(spatial_block), _p(v_covar), _p(vr), _p(vs), _p(vl))
+    return vr, vs, vl
+
+
+def cond_mean_convariance_opacity(means, covars, opacities, betas, query, dtype=np.float32):
+    means, covars = _c(means, dtype), _c(covars, dtype)
+    opacities, betas, query = _c(opacities, dtype), _c(betas, dtype), _c(query, dtype)
+    n, D = means.shape
+    om = np.zeros((n, 3), dtype)
+    oV = np.zeros((n, 3, 3), dtype)
+    oo = np.zeros((n, 1), dtype)
+    _fn("cond_fwd", dtype)(n, D, _p(means), _p(covars), _p(opacities), _p(betas), _p(query),
+                           _p(om), _p(oV), _p(oo))
+    return om, oV, oo
+
+
+def cond_mean_convariance_opacity_bwd(means, covars, opacities, betas, query, v_m, v_V, v_o,
+                                      dtype=np.float32, exact=False):
+    """exact=False reproduces the reference CUDA backward (including its
+    Cholesky-backward transposition); exact=True gives the true gradient."""
+    args = [_c(a, dtype) for a in (means, covars, opacities, betas, query, v_m, v_V, v_o)]
+    n, D = args[0].shape
+    gm = np.zeros((n, D), dtype)
+    gV = np.zeros((n, D, D), dtype)
+    go = np.zeros((n, 1), dtype)
+    gb = np.zeros((n, D - 3), dtype)
+    _fn("cond_bwd", dtype)(n, D, *[_p(a) for a in args], _p(gm), _p(gV), _p(go), _p(gb),
+                           int(exact))
+    return gm, gV, go, gb
+
+
+def fully_fused_projection(means, covars6, quats, scales, viewmats, Ks, width, height,
+                           eps2d=0.3, near_plane=0.01, far_plane=1e10, radius_clip=0.0,
+                           calc_compensations=False, dtype=np.float32):
+    means = _c(means, dtype)
+    covars6 = None if covars6 is None else _c(covars6, dtype)
+    quats = None if quats is None else _c(quats, dtype)
+    scales = None if scales is None else _c(scales, dtype)
+    viewmats, Ks = _c(viewmats, dtype), _c(Ks, dtype)
+    N, C = means.shape[0], viewmats.shape[0]
+    radii = np.zeros((C, N), np.int32)
+    m2 = np.zeros((C, N, 2), dtype)
+    d = np.zeros((C, N), dtype)
+    cn = np.zeros((C, N, 3), dtype)
+    cp = np.zeros((C, N), dtype) if calc_compensations else None
+    _fn("project_fwd", dtype)(C, N, _p(means), _p(covars6), _p(quats), _p(scales), _p(viewmats),
+                              _p(Ks), int(width), int(height), eps2d, near_plane, far_plane,
+                              radius_clip, _p(radii), _p(m2), _p(d), _p(cn), _p(cp))
+    return radii, m2, d, cn, cp
+
+
+def fully_fused_projection_bwd(means, covars6, quats, scales, viewmats, Ks, width, height,
+                               eps2d, radii, conics, comps, v_means2d, v_depths, v_conics,
+                               v_comps=None, dtype=np.float32):
+    means = _c(means, dtype)
+    covars6 = None if covars6 is None else _c(covars6, dtype)
+    quats = None if quats is None else _c(quats, dtype)
+    scales = None if scales is None else _c(scales, dtype)
+    viewmats, Ks = _c(viewmats, dtype), _c(Ks, dtype)
+    radii = _c(radii, np.int32)
+    conics = _c(conics, dtype)
+    comps = None if comps is None else _c(comps, dtype)
+    v_means2d, v_conics = _c(v_means2d, dtype), _c(v_conics, dtype)
+    v_depths = None if v_depths is None else _c(v_depths, dtype)
+    v_comps = None if v_comps is None else _c(v_comps, dtype)
+    N, C = means.shape[0], viewmats.shape[0]
+    vm = np.zeros((N, 3), dtype)
+    vc6 = np.zeros((N, 6), dtype) if covars6 is not None else None
+    vq = np.zeros((N, 4), dtype) if covars6 is None else None
+    vs = np.zeros((N, 3), dtype) if covars6 is None else None
+    vv = np.zeros((C, 4, 4), dtype)
+    _fn("project_bwd", dtype)(C, N, _p(means), _p(covars6), _p(quats), _p(scales), _p(viewmats),
+                              _p(Ks), int(width), int(height), eps2d, _p(radii), _p(conics),
+                              _p(comps), _p(v_means2d), _p(v_depths), _p(v_conics), _p(v_comps),
+                              _p(vm), _p(vc6), _p(vq), _p(vs), _p(vv))
+    return vm, vc6, vq, vs, vv
+
+
+def isect_tiles(means2d, radii, depths, tile_size, tile_width, tile_height, sort=True):
+    means2d = _c(means2d, np.float32)
+    radii = _c(radii, np.int32)
+    depths = _c(depths, np.float32)
+    C, N = radii.shape
+    tpg = np.zeros((C, N), np.int32)
+    L = lib()
+    n = L.ubso_isect_count(C, N, _p(means2d), _p(radii), tile_size, tile_width, tile_height,
+                           _p(tpg))
+    ids = np.zeros(n, np.int64)
+    fl = np.zeros(n, np.int32)
+    L.ubso_isect_emit_sort(C, N, _p(means2d), _p(radii), _p(depths), tile_size, tile_width,
+                           tile_height, _p(tpg), n, int(sort), _p(ids), _p(fl))
+    return tpg, ids, fl
+
+
+def isect_offset_encode(isect_ids, n_cameras, tile_width, tile_height):
+    isect_ids = _c(isect_ids, np.int64)
+    out = np.zeros((n_cameras, tile_height, tile_width), np.int32)
+    lib().ubso_offset_encode(len(isect_ids), _p(isect_ids), n_cameras, tile_width, tile_height,
+                             _p(out))
+    return out
+
+
+def rasterize_to_pixels(means2d, conics, colors, opacities, betas, width, height, tile_size,
+                        isect_offsets, flatten_ids, backgrounds=None, masks=None,
+                        dtype=np.float32):
+    means2d, conics, colors = _c(means2d, dtype), _c(conics, dtype), _c(colors, dtype)
+    opacities, betas = _c(opacities, dtype), _c(betas, dtype)
+    offs = _c(isect_offsets, np.int32)
+    fl = _c(flatten_ids, np.int32)
+    bg = None if backgrounds is None else _c(backgrounds, dtype)
+    mk = None if masks is None else _c(masks, np.uint8)
+    C, th, tw = offs.shape
+    N, cd = colors.shape[1], colors.shape[2]
+    oc = np.zeros((C, height, width, cd), dtype)
+    oa = np.zeros((C, height, width, 1), dtype)
+    li = np.zeros((C, height, width), np.int32)
+    _fn("raster_fwd", dtype)(C, N, cd, len(fl), _p(means2d), _p(conics), _p(colors),
+                             _p(opacities), _p(betas), _p(bg), _p(mk), int(width), int(height),
+                             int(tile_size), tw, th, _p(offs), _p(fl), _p(oc), _p(oa), _p(li))
+    return oc, oa, li
+
+
+def rasterize_to_pixels_bwd(means2d, conics, colors, opacities, betas, width, height,
+                            tile_size, isect_offsets, flatten_ids, render_alphas, last_ids,
+                            v_colors, v_alphas, backgrounds=None, masks=None, dtype=np.float32):
+    means2d, conics, colors = _c(means2d, dtype), _c(conics, dtype), _c(colors, dtype)
+    opacities, betas = _c(opacities, dtype), _c(betas, dtype)
+    offs = _c(isect_offsets, np.int32)
+    fl = _c(flatten_ids, np.int32)
+    bg = None if backgrounds is None else _c(backgrounds, dtype)
+    mk = None if masks is None else _c(masks, np.uint8)
+    ra, li = _c(render_alphas, dtype), _c(last_ids, np.int32)
+    vc, va = _c(v_colors, dtype), _c(v_alphas, dtype)
+    C, th, tw = offs.shape
+    N, cd = colors.shape[1], colors.shape[2]
+    vm2 = np.zeros((C, N, 2), dtype)
+    vcn = np.zeros((C, N, 3), dtype)
+    vcol = np.zeros((C, N, cd), dtype)
+    vo = np.zeros((C, N), dtype)
+    vb = np.zeros((C, N), dtype)
+    _fn("raster_bwd", dtype)(C, N, cd, len(fl), _p(means2d), _p(conics), _p(colors),
+                             _p(opacities), _p(betas), _p(bg), _p(mk), int(width), int(height),
+                             int(tile_size), tw, th, _p(offs), _p(fl), _p(ra), _p(li), _p(vc),
+                             _p(va), _p(vm2), _p(vcn), _p(vcol), _p(vo), _p(vb))
+    return vm2, vcn, vcol, vo, vb
