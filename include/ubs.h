@@ -1,0 +1,186 @@
+/*
+ * ubs.h -- C ABI of the GB300 (sm_103a) Universal Beta Splatting rasteriser.
+ *
+ * Conventions (all entry points):
+ *   - Plain device pointers and sizes; no framework types.  `stream` is a
+ *     cudaStream_t passed as void* (NULL = legacy default stream).
+ *   - The caller owns every buffer.  The library allocates nothing: scratch
+ *     memory is a caller-provided workspace whose size comes from the matching
+ *     *_workspace_bytes() query.
+ *   - float32 tensors are contiguous, row-major; int tensors int32 unless
+ *     stated.  Shapes are given in the comment of each function.
+ *   - Return 0 (UBS_OK) on success or a negative UBS_ERR_* code; the message
+ *     of the calling thread's last failure is returned by ubs_last_error().
+ *   - Kernels never trap.  Device-side waits are bounded; a wait that runs out
+ *     or an invalid input discovered on the device sets a status word that the
+ *     synchronising entry points report as UBS_ERR_DEVICE.
+ *
+ * Each declaration names the reference operator it replaces
+ * (paths inside RongLiu-Leo/universal-beta-splatting).
+ */
+#ifndef UBS_GB300_H
+#define UBS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define UBS_OK 0
+#define UBS_ERR_INVALID (-1)     /* bad argument (shape, size, pointer)         */
+#define UBS_ERR_CUDA (-2)        /* a CUDA runtime call or kernel launch failed */
+#define UBS_ERR_UNSUPPORTED (-3) /* valid in the reference, not supported here  */
+#define UBS_ERR_OVERFLOW (-4)    /* a caller buffer or workspace is too small   */
+#define UBS_ERR_DEVICE (-5)      /* a kernel reported a device-side status      */
+
+/* Message of the calling thread's last failure ("" if none). */
+const char *ubs_last_error(void);
+/* ABI version of this library (bumped on any signature change). */
+int ubs_abi_version(void);
+
+/* ------------------------------------------------------------------ a2 ---
+ * R = I + A(a01, a02, a12): submodules/gsplat/cuda/_wrapper.py:34
+ * (l_triangle_to_rotmat), kernels l_triagnle_to_rotmat_fwd.cu:8 / _bwd.cu:8.
+ * l_triangle [n, row_stride] (first 3 entries of each row used), rotmats [n,3,3].
+ * v_l_triangle [n, 3]. */
+int ubs_l_triangle_to_rotmat_fwd(int64_t n, const float *l_triangle, int64_t row_stride,
+                                 float *rotmats, void *stream);
+int ubs_l_triangle_to_rotmat_bwd(int64_t n, const float *v_rotmats, float *v_l_triangle,
+                                 void *stream);
+
+/* ------------------------------------------------------------------ a3 ---
+ * Sigma = L L^T from rotation, scale and lower-triangle parameters:
+ * _wrapper.py:39 (rot_scale_l_triangle_to_covar), kernels
+ * rot_scale_l_triangle_to_covar_fwd.cu:8 / _bwd.cu:8.
+ * rot [n,3,3], scale [n,dim], l_triangle [n, dim*(dim-1)/2], rest_i/rest_j
+ * device int32 [m_rest]; covar [n,dim,dim] or [n,3,3] if spatial_block.
+ * 3 <= dim <= 11. */
+int ubs_rot_scale_l_triangle_to_covar_fwd(int64_t n, int32_t dim, const float *rot,
+                                          const float *scale, const float *l_triangle,
+                                          const int32_t *rest_i, const int32_t *rest_j,
+                                          int32_t m_rest, int32_t spatial_block, float *covar,
+                                          void *stream);
+int ubs_rot_scale_l_triangle_to_covar_bwd(int64_t n, int32_t dim, const float *rot,
+                                          const float *scale, const float *l_triangle,
+                                          const int32_t *rest_i, const int32_t *rest_j,
+                                          int32_t m_rest, int32_t spatial_block,
+                                          const float *v_covar, float *v_rot, float *v_scale,
+                                          float *v_l_triangle, void *stream);
+
+/* ------------------------------------------------------------------ a4 ---
+ * Conditioning of an N-D Beta primitive on its view query: _wrapper.py:18
+ * (cond_mean_convariance_opacity), kernels cond_mean_convariance_opacity_fwd.cu:107
+ * / _bwd.cu:102.  means [n,dim], covars [n,dim,dim], opacities [n], betas and
+ * query [n,dim-3]; out_means [n,3], out_covars [n,3,3], out_opacities [n].
+ * 4 <= dim <= 11.  exact == 0 reproduces the reference backward bit-for-bit in
+ * formula (including its transposed Cholesky-backward factor); exact != 0 gives
+ * the true gradient of the forward. */
+int ubs_cond_fwd(int64_t n, int32_t dim, const float *means, const float *covars,
+                 const float *opacities, const float *betas, const float *query,
+                 float *out_means, float *out_covars, float *out_opacities, void *stream);
+int ubs_cond_bwd(int64_t n, int32_t dim, const float *means, const float *covars,
+                 const float *opacities, const float *betas, const float *query,
+                 const float *v_out_means, const float *v_out_covars,
+                 const float *v_out_opacities, float *v_means, float *v_covars,
+                 float *v_opacities, float *v_betas, int32_t exact, void *stream);
+
+/* ------------------------------------------------------------------ a6 ---
+ * EWA perspective projection: _wrapper.py:185 (fully_fused_projection),
+ * kernels fully_fused_projection_fwd.cu:20 / _bwd.cu:20.
+ * means [N,3]; covars either [N,6] (upper triangle, covar_layout = 6) or
+ * [N,3,3] (covar_layout = 9); or covars == NULL and quats [N,4] + scales [N,3].
+ * viewmats [C,4,4] (world-to-camera, row-major), Ks [C,3,3].
+ * radii [C,N] int32, means2d [C,N,2], depths [C,N], conics [C,N,3],
+ * compensations [C,N] or NULL.  Culled entries get radius 0 and zeros.
+ * Backward: v_* of the outputs in, gradients out (overwritten, summed over
+ * cameras); v_covars uses covar_layout (for 9 the upper triangle holds the
+ * gradient of the packed entries and the strict lower triangle is zero);
+ * v_viewmats [C,4,4] or NULL. */
+int ubs_projection_fwd(int32_t C, int64_t N, const float *means, const float *covars,
+                       int32_t covar_layout, const float *quats, const float *scales,
+                       const float *viewmats, const float *Ks, int32_t width, int32_t height,
+                       float eps2d, float near_plane, float far_plane, float radius_clip,
+                       int32_t *radii, float *means2d, float *depths, float *conics,
+                       float *compensations, void *stream);
+int ubs_projection_bwd(int32_t C, int64_t N, const float *means, const float *covars,
+                       int32_t covar_layout, const float *quats, const float *scales,
+                       const float *viewmats, const float *Ks, int32_t width, int32_t height,
+                       float eps2d, const int32_t *radii, const float *conics,
+                       const float *compensations, const float *v_means2d,
+                       const float *v_depths, const float *v_conics,
+                       const float *v_compensations, float *v_means, float *v_covars,
+                       float *v_quats, float *v_scales, float *v_viewmats, void *stream);
+
+/* ------------------------------------------------------------- a7 / a8 ---
+ * Tile intersection: _wrapper.py:286 (isect_tiles), kernel isect_tiles.cu:17-285,
+ * and offsets _wrapper.py:347 (isect_offset_encode), isect_tiles.cu:287-367.
+ * Step 1 (synchronises the stream, like the reference's .item()):
+ *   tiles_per_gauss [C,N], isect_offsets [C,tile_height,tile_width] and the
+ *   intersection count.  Workspace: ubs_isect_count_workspace_bytes().
+ * Step 2: isect_ids [n_isects] int64 (cam | tile | depth bits) and
+ *   flatten_ids [n_isects] int32, sorted like the reference's stable radix sort
+ *   when sort != 0, else in the reference's generation order.  Workspace:
+ *   ubs_isect_sort_workspace_bytes(); it must begin with the count workspace
+ *   of step 1, unchanged.
+ * Depths of visible primitives must be non-negative (the reference's key then
+ * overflows into the tile field); a negative one makes step 1 fail. */
+size_t ubs_isect_count_workspace_bytes(int32_t C, int64_t N, int32_t n_tiles);
+size_t ubs_isect_sort_workspace_bytes(int32_t C, int64_t N, int32_t n_tiles, int64_t n_isects);
+int ubs_isect_count(int32_t C, int64_t N, const float *means2d, const int32_t *radii,
+                    const float *depths, int32_t tile_size, int32_t tile_width,
+                    int32_t tile_height, int32_t *tiles_per_gauss, int32_t *isect_offsets,
+                    int64_t *n_isects, void *workspace, size_t workspace_bytes, void *stream);
+int ubs_isect_emit(int32_t C, int64_t N, const float *means2d, const int32_t *radii,
+                   const float *depths, int32_t tile_size, int32_t tile_width,
+                   int32_t tile_height, const int32_t *tiles_per_gauss,
+                   const int32_t *isect_offsets, int64_t n_isects, int32_t sort,
+                   int64_t *isect_ids, int32_t *flatten_ids, void *workspace,
+                   size_t workspace_bytes, void *stream);
+/* offsets [C,tile_height,tile_width] from sorted isect_ids [n_isects]. */
+int ubs_isect_offset_encode(int64_t n_isects, const int64_t *isect_ids, int32_t C,
+                            int32_t tile_width, int32_t tile_height, int32_t *offsets,
+                            void *stream);
+
+/* ------------------------------------------------------------ a9 / a10 ---
+ * Per-tile Beta-kernel blend: _wrapper.py:366 (rasterize_to_pixels),
+ * kernels rasterize_to_pixels_fwd.cu:17 / _bwd.cu:17.
+ * means2d [C,N,2], conics [C,N,3], colors [C,N,channels], opacities and betas
+ * [C,N], backgrounds [C,channels] or NULL, masks [C,tile_height,tile_width]
+ * uint8 or NULL, isect_offsets [C,tile_height,tile_width], flatten_ids
+ * [n_isects].  Forward outputs: render_colors [C,H,W,channels], render_alphas
+ * [C,H,W], last_ids [C,H,W] int32.  Backward outputs (overwritten):
+ * v_means2d, v_conics, v_colors, v_opacities, v_betas; the background
+ * gradient is left to the caller, as in the reference.
+ * channels in [1, 33]; tile_size in {8, 16, 24, 32}.
+ * Workspace: ubs_raster_workspace_bytes(n_isects, channels). */
+size_t ubs_raster_workspace_bytes(int64_t n_isects, int32_t channels);
+int ubs_raster_fwd(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
+                   const float *means2d, const float *conics, const float *colors,
+                   const float *opacities, const float *betas, const float *backgrounds,
+                   const uint8_t *masks, int32_t width, int32_t height, int32_t tile_size,
+                   int32_t tile_width, int32_t tile_height, const int32_t *isect_offsets,
+                   const int32_t *flatten_ids, float *render_colors, float *render_alphas,
+                   int32_t *last_ids, void *workspace, size_t workspace_bytes, void *stream);
+int ubs_raster_bwd(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
+                   const float *means2d, const float *conics, const float *colors,
+                   const float *opacities, const float *betas, const float *backgrounds,
+                   const uint8_t *masks, int32_t width, int32_t height, int32_t tile_size,
+                   int32_t tile_width, int32_t tile_height, const int32_t *isect_offsets,
+                   const int32_t *flatten_ids, const float *render_alphas,
+                   const int32_t *last_ids, const float *v_render_colors,
+                   const float *v_render_alphas, float *v_means2d, float *v_conics,
+                   float *v_colors, float *v_opacities, float *v_betas, void *workspace,
+                   size_t workspace_bytes, void *stream);
+
+/* Device status word of the last raster call on `workspace` (0 = clean);
+ * synchronises the stream.  Bits: 1 wait timeout, 2 negative depth,
+ * 4 overflow. */
+int ubs_raster_status(const void *workspace, uint32_t *status, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* UBS_GB300_H */

@@ -1,0 +1,298 @@
+"""GPU parity: every operator of the rasteriser path, run through the C ABI
+(libubs_gb300.so), against the CPU oracle on the same seeded inputs.
+
+Tolerances (FP32 path): images within 1e-5 max abs; tile ids, counts, sorted
+orders and offsets bit-exact; gradients within 1e-4 relative (L2 over each
+tensor), element-wise within rtol 2e-3 / atol scaled by the tensor's range.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle as orc
+from scenes import beta_params, intrinsics, look_at, orbit_camera, projected_scene, rest_indices
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+
+
+def npy(t):
+    return t.detach().cpu().numpy()
+
+
+def grad_close(a, b, what, rel_l2=1e-4, rtol=2e-3):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    scale = max(np.abs(b).max(), 1e-30)
+    l2 = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+    assert l2 <= rel_l2, "%s: relative L2 error %.3g" % (what, l2)
+    bad = np.abs(a - b) > rtol * np.abs(b) + 1e-4 * scale
+    assert bad.mean() < 1e-3, "%s: %d elements outside tolerance (max abs diff %.3g)" % (
+        what, bad.sum(), np.abs(a - b).max())
+
+
+# ------------------------------------------------------------- a2, a3, a4
+@pytest.mark.parametrize("D", [6, 7])
+def test_rotmat_covar_fwd_bwd(D):
+    from gsplat.cuda._wrapper import l_triangle_to_rotmat, rot_scale_l_triangle_to_covar
+    p = beta_params(3000, D, seed=1)
+    ri, rj = rest_indices(D)
+    lt = p["l_triangle"].to(DEV).requires_grad_(True)
+    sc = torch.nn.functional.softplus(p["scale"]).to(DEV).requires_grad_(True)
+    R = l_triangle_to_rotmat(lt[:, :3])
+    cov = rot_scale_l_triangle_to_covar(R, sc, lt, ri.to(DEV), rj.to(DEV))
+    R_o = orc.l_triangle_to_rotmat(npy(lt))
+    np.testing.assert_array_equal(npy(R), R_o)
+    cov_o = orc.rot_scale_l_triangle_to_covar(R_o, npy(sc), npy(lt), npy(ri), npy(rj))
+    np.testing.assert_allclose(npy(cov), cov_o, rtol=1e-5, atol=1e-7)
+    sp = rot_scale_l_triangle_to_covar(R, sc, lt, ri.to(DEV), rj.to(DEV), spatial_block=True)
+    sp_o = orc.rot_scale_l_triangle_to_covar(R_o, npy(sc), npy(lt), npy(ri), npy(rj), True)
+    np.testing.assert_allclose(npy(sp), sp_o, rtol=1e-5, atol=1e-7)
+    g = torch.randn(cov.shape, generator=torch.Generator().manual_seed(2)).to(DEV)
+    (cov * g).sum().backward()
+    vr, vs, vl = orc.rot_scale_l_triangle_to_covar_bwd(R_o, npy(sc), npy(lt), npy(ri), npy(rj),
+                                                       npy(g))
+    vl3 = orc.l_triangle_to_rotmat_bwd(vr)
+    vl_total = vl.copy()
+    vl_total[:, :3] += vl3
+    grad_close(npy(sc.grad), vs, "v_scale")
+    grad_close(npy(lt.grad), vl_total, "v_l_triangle")
+
+
+@pytest.mark.parametrize("D", [6, 7])
+@pytest.mark.parametrize("mode", ["reference", "exact"])
+def test_cond_fwd_bwd(D, mode):
+    from gsplat.cuda import _wrapper as W
+    p = beta_params(4000, D, seed=3)
+    ri, rj = rest_indices(D)
+    R = orc.l_triangle_to_rotmat(npy(p["l_triangle"]))
+    cov = orc.rot_scale_l_triangle_to_covar(R, npy(torch.nn.functional.softplus(p["scale"])),
+                                            npy(p["l_triangle"]), npy(ri), npy(rj))
+    means = torch.cat([p["xyz"], p["mean"]], 1)
+    opac = torch.sigmoid(p["opacity"])
+    betas = (4 * torch.exp(p["beta"]))[:, 1:]
+    q = torch.nn.functional.normalize(torch.randn(4000, 3, generator=torch.Generator().manual_seed(4)), dim=-1)
+    if D == 7:
+        q = torch.cat([q, torch.rand(4000, 1, generator=torch.Generator().manual_seed(5))], 1)
+    args_t = [t.to(DEV).requires_grad_(i < 4) for i, t in
+              enumerate([means, torch.tensor(cov), opac, betas, q])]
+    prev = W.get_cond_grad_mode()
+    W.set_cond_grad_mode(mode)
+    try:
+        m, V, o = W.cond_mean_convariance_opacity(*args_t)
+        mo, Vo, oo = orc.cond_mean_convariance_opacity(*[npy(t) for t in args_t])
+        np.testing.assert_allclose(npy(m), mo, rtol=1e-4, atol=1e-5)
+        np.testing.assert_allclose(npy(V), Vo, rtol=1e-4, atol=1e-6)
+        np.testing.assert_allclose(npy(o), oo, rtol=1e-3, atol=1e-6)
+        g = torch.Generator().manual_seed(6)
+        gm, gV, go = (torch.randn(m.shape, generator=g), torch.randn(V.shape, generator=g),
+                      torch.randn(o.shape, generator=g))
+        ((m * gm.to(DEV)).sum() + (V * gV.to(DEV)).sum() + (o * go.to(DEV)).sum()).backward()
+        ref = orc.cond_mean_convariance_opacity_bwd(*[npy(t) for t in args_t], npy(gm), npy(gV),
+                                                    npy(go), exact=(mode == "exact"))
+    finally:
+        W.set_cond_grad_mode(prev)
+    for t, r, nm in zip(args_t[:4], ref, ("v_means", "v_covars", "v_opac", "v_betas")):
+        grad_close(npy(t.grad), r, nm, rel_l2=2e-4)
+
+
+# ------------------------------------------------------------------- a6
+@pytest.mark.parametrize("layout", [6, 9, "quat"])
+def test_projection_fwd_bwd(layout):
+    from gsplat.cuda._wrapper import fully_fused_projection
+    g = torch.Generator().manual_seed(7)
+    N, C, W, H = 5000, 2, 320, 240
+    means = (torch.rand(N, 3, generator=g) * 2 - 1) * 1.5
+    Lm = torch.randn(N, 3, 3, generator=g) * 0.03
+    cov33 = Lm @ Lm.transpose(1, 2) + 1e-4 * torch.eye(3)
+    vms = torch.stack([look_at((0.5, 0.3, -4.0)), orbit_camera(g, 4.0)])
+    Ks = torch.stack([intrinsics(300, 300, 160, 120)] * C)
+    quats = torch.randn(N, 4, generator=g)
+    scales = torch.exp(torch.randn(N, 3, generator=g) * 0.5 - 3)
+    if layout == "quat":
+        cov_in, q_in, s_in = None, quats.to(DEV).requires_grad_(True), scales.to(DEV).requires_grad_(True)
+        c6 = None
+    else:
+        c6 = cov33[:, [0, 0, 0, 1, 1, 2], [0, 1, 2, 1, 2, 2]]
+        cov_in = (c6 if layout == 6 else cov33).to(DEV).requires_grad_(True)
+        q_in = s_in = None
+    mt = means.to(DEV).requires_grad_(True)
+    vt = vms.to(DEV).requires_grad_(True)
+    radii, m2, d, cn, _ = fully_fused_projection(mt, cov_in, q_in, s_in, vt, Ks.to(DEV), W, H)
+    r_o, m2_o, d_o, cn_o, _ = orc.fully_fused_projection(
+        npy(means), None if c6 is None else npy(c6), None if c6 is not None else npy(quats),
+        None if c6 is not None else npy(scales), npy(vms), npy(Ks), W, H)
+    rr = npy(radii)
+    # radius = ceil(sqrt(.)) can move by one at integer boundaries between the
+    # GPU (fast-math sqrt) and the CPU oracle; culling decisions must agree
+    assert ((rr > 0) == (r_o > 0)).mean() > 0.999
+    assert (np.abs(rr - r_o) <= 1).all()
+    assert (rr == r_o).mean() > 0.995
+    v = (rr > 0) & (r_o > 0)
+    np.testing.assert_allclose(npy(m2)[v], m2_o[v], rtol=1e-5, atol=1e-3)
+    np.testing.assert_allclose(npy(d)[v], d_o[v], rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(npy(cn)[v], cn_o[v], rtol=2e-4, atol=1e-7)
+    gg = torch.Generator().manual_seed(8)
+    w2 = torch.randn(m2.shape, generator=gg)
+    wd = torch.randn(d.shape, generator=gg)
+    wc = torch.randn(cn.shape, generator=gg) * 1e-2
+    ((m2 * w2.to(DEV)).sum() + (d * wd.to(DEV)).sum() + (cn * wc.to(DEV)).sum()).backward()
+    vm_o, vc6_o, vq_o, vs_o, vv_o = orc.fully_fused_projection_bwd(
+        npy(means), None if c6 is None else npy(c6), None if c6 is not None else npy(quats),
+        None if c6 is not None else npy(scales), npy(vms), npy(Ks), W, H, 0.3, npy(radii),
+        npy(cn), None, npy(w2), npy(wd), npy(wc))
+    grad_close(npy(mt.grad), vm_o, "v_means", rel_l2=2e-4)
+    grad_close(npy(vt.grad), vv_o, "v_viewmats", rel_l2=2e-4)
+    if layout == 6:
+        grad_close(npy(cov_in.grad), vc6_o, "v_covars6", rel_l2=2e-4)
+    elif layout == 9:
+        full = np.zeros((N, 3, 3))
+        for k, (i, j) in enumerate([(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)]):
+            full[:, i, j] = vc6_o[:, k]
+        grad_close(npy(cov_in.grad), full, "v_covars33", rel_l2=2e-4)
+    else:
+        grad_close(npy(q_in.grad), vq_o, "v_quats", rel_l2=2e-4)
+        grad_close(npy(s_in.grad), vs_o, "v_scales", rel_l2=2e-4)
+
+
+# --------------------------------------------------------------- a7 / a8
+@pytest.mark.parametrize("C,N,W,H,ts", [(1, 20000, 640, 480, 16), (3, 7000, 333, 250, 16),
+                                        (2, 5000, 256, 200, 8), (1, 3000, 300, 300, 32)])
+def test_isect_bit_exact(C, N, W, H, ts):
+    from gsplat.cuda._wrapper import isect_offset_encode, isect_tiles
+    s = projected_scene(N, W, H, C=C, seed=C * 100 + ts)
+    tw, th = (W + ts - 1) // ts, (H + ts - 1) // ts
+    radii = s["radii"].clone()
+    radii[:, ::11] = 0
+    # equal depths exercise the tie order (flatten index)
+    depths = s["depths"].clone()
+    depths[:, 1::9] = 3.0
+    tpg, ids, fl = isect_tiles(s["means2d"].to(DEV), radii.to(DEV), depths.to(DEV), ts, tw, th)
+    tpg_o, ids_o, fl_o = orc.isect_tiles(npy(s["means2d"]), npy(radii), npy(depths), ts, tw, th)
+    np.testing.assert_array_equal(npy(tpg), tpg_o)
+    np.testing.assert_array_equal(npy(ids), ids_o)
+    np.testing.assert_array_equal(npy(fl), fl_o)
+    offs = isect_offset_encode(ids, C, tw, th)
+    np.testing.assert_array_equal(npy(offs), orc.isect_offset_encode(ids_o, C, tw, th))
+    # unsorted: the reference's generation order
+    _, ids_u, fl_u = isect_tiles(s["means2d"].to(DEV), radii.to(DEV), depths.to(DEV), ts, tw,
+                                 th, sort=False)
+    _, ids_uo, fl_uo = orc.isect_tiles(npy(s["means2d"]), npy(radii), npy(depths), ts, tw, th,
+                                       sort=False)
+    np.testing.assert_array_equal(npy(ids_u), ids_uo)
+    np.testing.assert_array_equal(npy(fl_u), fl_uo)
+
+
+def test_isect_long_buckets_and_empty():
+    """Buckets longer than the shared-memory sort (4096) take the merge path."""
+    from gsplat.cuda._wrapper import isect_offset_encode, isect_tiles
+    N, W, H, ts = 30000, 64, 64, 16
+    g = torch.Generator().manual_seed(11)
+    m2 = torch.rand(1, N, 2, generator=g) * 64
+    radii = torch.full((1, N), 100, dtype=torch.int32)  # every primitive covers every tile
+    depths = torch.rand(1, N, generator=g) * 4 + 0.5
+    depths[0, ::5] = 2.0
+    tpg, ids, fl = isect_tiles(m2.to(DEV), radii.to(DEV), depths.to(DEV), ts, 4, 4)
+    tpg_o, ids_o, fl_o = orc.isect_tiles(npy(m2), npy(radii), npy(depths), ts, 4, 4)
+    assert len(ids_o) == 16 * N
+    np.testing.assert_array_equal(npy(ids), ids_o)
+    np.testing.assert_array_equal(npy(fl), fl_o)
+    # nothing visible
+    tpg, ids, fl = isect_tiles(m2.to(DEV), torch.zeros_like(radii).to(DEV), depths.to(DEV), ts,
+                               4, 4)
+    assert ids.numel() == 0 and fl.numel() == 0 and int(tpg.abs().sum()) == 0
+    offs = isect_offset_encode(ids, 1, 4, 4)
+    assert int(offs.abs().sum()) == 0
+
+
+def test_isect_rejects_negative_depth():
+    from gsplat.cuda._wrapper import isect_tiles
+    s = projected_scene(100, 64, 64, seed=3)
+    d = s["depths"].clone()
+    d[0, 5] = -1.0
+    with pytest.raises(RuntimeError, match="negative depth"):
+        isect_tiles(s["means2d"].to(DEV), s["radii"].to(DEV), d.to(DEV), 16, 4, 4)
+
+
+# ------------------------------------------------------------- a9 / a10
+def _blend_inputs(N, W, H, C, seed, ts, channels=3, big_frac=0.0):
+    from gsplat.cuda._wrapper import isect_offset_encode, isect_tiles
+    s = projected_scene(N, W, H, C=C, seed=seed, big_frac=big_frac)
+    g = torch.Generator().manual_seed(seed + 1)
+    colors = torch.rand(C, N, channels, generator=g)
+    tw, th = (W + ts - 1) // ts, (H + ts - 1) // ts
+    _, ids, fl = isect_tiles(s["means2d"].to(DEV), s["radii"].to(DEV), s["depths"].to(DEV), ts,
+                             tw, th)
+    offs = isect_offset_encode(ids, C, tw, th)
+    return s, colors, offs, fl
+
+
+@pytest.mark.parametrize("C,N,W,H,ts,channels,bg", [
+    (1, 4000, 256, 192, 16, 3, False),
+    (1, 4000, 256, 192, 16, 3, True),
+    (2, 3000, 200, 150, 16, 4, True),
+    (1, 2500, 160, 120, 8, 1, False),
+    (1, 2500, 160, 120, 32, 3, True),
+    (1, 2000, 128, 96, 16, 8, True),
+    (1, 1500, 128, 96, 16, 33, False),
+    (1, 1500, 96, 80, 16, 6, True),    # padded to 8
+    (1, 1200, 96, 80, 16, 40, False),  # split into 32-channel chunks
+])
+def test_blend_fwd_bwd(C, N, W, H, ts, channels, bg):
+    from gsplat.cuda._wrapper import rasterize_to_pixels
+    s, colors, offs, fl = _blend_inputs(N, W, H, C, seed=N + W, ts=ts, channels=channels)
+    g = torch.Generator().manual_seed(99)
+    bgs = torch.rand(C, channels, generator=g) if bg else None
+    ts_in = [s["means2d"], s["conics"], colors, s["opacities"], s["betas"]]
+    ts_dev = [t.to(DEV).requires_grad_(True) for t in ts_in]
+    bg_dev = bgs.to(DEV).requires_grad_(True) if bg else None
+    rc, ra = rasterize_to_pixels(*ts_dev, W, H, ts, offs, fl, backgrounds=bg_dev)
+    oc, oa, li = orc.rasterize_to_pixels(*[npy(t) for t in ts_in], W, H, ts, npy(offs), npy(fl),
+                                         backgrounds=None if bgs is None else npy(bgs))
+    assert np.abs(npy(rc) - oc).max() < 1e-5, np.abs(npy(rc) - oc).max()
+    assert np.abs(npy(ra) - oa).max() < 1e-5
+    wc = torch.randn(rc.shape, generator=g)
+    wa = torch.randn(ra.shape, generator=g)
+    ((rc * wc.to(DEV)).sum() + (ra * wa.to(DEV)).sum()).backward()
+    ref = orc.rasterize_to_pixels_bwd(*[npy(t) for t in ts_in], W, H, ts, npy(offs), npy(fl),
+                                      oa, li, npy(wc), npy(wa),
+                                      backgrounds=None if bgs is None else npy(bgs))
+    for t, r, nm in zip(ts_dev, ref, ("v_means2d", "v_conics", "v_colors", "v_opac", "v_betas")):
+        grad_close(npy(t.grad), r, nm)
+    if bg:
+        v_bg = (wc * (1 - torch.tensor(oa))).sum(dim=(1, 2))
+        np.testing.assert_allclose(npy(bg_dev.grad), npy(v_bg), rtol=1e-4, atol=1e-3)
+
+
+def test_blend_termination_and_masks():
+    """Opaque scene: early termination (T <= 1e-4), the 0.999 clamp and tile masks."""
+    from gsplat.cuda._wrapper import rasterize_to_pixels
+    C, N, W, H, ts = 1, 3000, 128, 128, 16
+    s, colors, offs, fl = _blend_inputs(N, W, H, C, seed=5, ts=ts)
+    opac = torch.full_like(s["opacities"], 0.9995)  # clamps to 0.999
+    betas = torch.full_like(s["betas"], 0.2)
+    masks = torch.rand(C, H // ts, W // ts, generator=torch.Generator().manual_seed(1)) > 0.3
+    rc, ra = rasterize_to_pixels(s["means2d"].to(DEV), s["conics"].to(DEV), colors.to(DEV),
+                                 opac.to(DEV), betas.to(DEV), W, H, ts, offs, fl,
+                                 masks=masks.to(DEV))
+    oc, oa, li = orc.rasterize_to_pixels(npy(s["means2d"]), npy(s["conics"]), npy(colors),
+                                         npy(opac), npy(betas), W, H, ts, npy(offs), npy(fl),
+                                         masks=npy(masks))
+    assert np.abs(npy(rc) - oc).max() < 1e-5
+    m = np.repeat(np.repeat(npy(masks), ts, 1), ts, 2)[..., None]
+    assert np.abs((npy(ra) - oa) * m).max() < 1e-5
+    assert (oa[m.astype(bool)] > 0.99).mean() > 0.5  # the scene is mostly opaque
+
+
+def test_blend_empty():
+    from gsplat.cuda._wrapper import rasterize_to_pixels
+    C, N, W, H = 1, 10, 50, 40
+    z = torch.zeros(C, N, device=DEV)
+    offs = torch.zeros(C, 3, 4, dtype=torch.int32, device=DEV)
+    fl = torch.zeros(0, dtype=torch.int32, device=DEV)
+    bg = torch.tensor([[0.1, 0.2, 0.3]], device=DEV)
+    rc, ra = rasterize_to_pixels(torch.zeros(C, N, 2, device=DEV), torch.ones(C, N, 3, device=DEV),
+                                 torch.rand(C, N, 3, device=DEV), z, z, W, H, 16, offs, fl,
+                                 backgrounds=bg)
+    assert torch.allclose(rc, bg.view(1, 1, 1, 3).expand_as(rc))
+    assert float(ra.abs().max()) == 0.0

@@ -1,0 +1,716 @@
+// raster.cu -- per-tile Beta-kernel blend, forward and backward, for sm_103a.
+//
+// Reference: submodules/gsplat/cuda/csrc/rasterize_to_pixels_fwd.cu:17-191 and
+// rasterize_to_pixels_bwd.cu:17-276.  The per-pixel arithmetic (sigma, alpha,
+// transmittance, exclusive termination at T <= 1e-4, back-to-front
+// transmittance recovery from 1 - render_alpha) follows the reference so that
+// images agree to FP32 rounding.  The data movement is new:
+//   * a pack pass writes one 32-byte geometry record (+16-byte colour record
+//     for <= 4 channels) per sorted intersection, so every tile reads its
+//     front-to-back list as one contiguous span;
+//   * each CTA streams its span through shared memory with bulk async copies
+//     (cp.async.bulk + mbarrier, double-buffered, bounded waits);
+//   * every batch, each record's ellipse bounding box is tested against the
+//     8x4-pixel footprint of every warp and turned into per-warp bitmasks by
+//     ballot, so a warp only visits records that can touch its pixels;
+//   * the backward sums the 7 + channels gradients of a record over a warp with
+//     a transpose reduction (16 shuffles for 16 values), accumulates warps in
+//     shared memory and issues one global atomic per (tile, record, value).
+#include <cstdio>
+
+#include "ubs_common.cuh"
+
+namespace ubs {
+
+struct __align__(16) GeoRec {
+    float x, y, opac, beta;
+    float cxx, cxy, cyy;
+    int32_t gid;
+};
+static_assert(sizeof(GeoRec) == 32, "GeoRec must be 32 bytes");
+
+constexpr uint32_t DEV_ERR_BAD_INDEX = 8u;
+
+struct RasterArgs {
+    int C, W, H, TS, TW, TH, n_tiles;
+    int64_t n_isects, n_prims; // n_prims = C * N
+    const int32_t *offsets;
+    const GeoRec *recs;
+    const float4 *rcols; // packed colours (channels <= 4) or nullptr
+    const float *colors; // [C*N, CD], gathered when rcols == nullptr
+    const float *bg;
+    const uint8_t *masks;
+    // forward outputs
+    float *out_c;
+    float *out_a;
+    int32_t *last_ids;
+    // backward inputs / outputs
+    const float *render_alphas;
+    const int32_t *last_in;
+    const float *v_out_c;
+    const float *v_out_a;
+    float *v_m2, *v_cn, *v_col, *v_op, *v_be;
+    uint32_t *status;
+};
+
+// ---------------------------------------------------------------- packing
+template <int CD, bool PACK>
+__global__ void pack_records_kernel(int64_t T, int64_t n_prims, const int32_t *__restrict__ fl,
+                                    const float *__restrict__ m2, const float *__restrict__ cn,
+                                    const float *__restrict__ op, const float *__restrict__ be,
+                                    const float *__restrict__ col, GeoRec *__restrict__ recs,
+                                    float4 *__restrict__ rcols, uint32_t *status) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < T; i += stride) {
+        int32_t g = fl[i];
+        if (g < 0 || g >= n_prims) {
+            atomicOr(status, DEV_ERR_BAD_INDEX);
+            g = 0;
+        }
+        float4 a, b;
+        a.x = m2[2 * (int64_t)g];
+        a.y = m2[2 * (int64_t)g + 1];
+        a.z = op[g];
+        a.w = be[g];
+        b.x = cn[3 * (int64_t)g];
+        b.y = cn[3 * (int64_t)g + 1];
+        b.z = cn[3 * (int64_t)g + 2];
+        b.w = __int_as_float(g);
+        float4 *dst = reinterpret_cast<float4 *>(recs + i);
+        dst[0] = a;
+        dst[1] = b;
+        if (PACK) {
+            float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+            const float *cp = col + (int64_t)g * CD;
+            c.x = cp[0];
+            if (CD > 1) c.y = cp[1];
+            if (CD > 2) c.z = cp[2];
+            if (CD > 3) c.w = cp[3];
+            rcols[i] = c;
+        }
+    }
+}
+
+// ------------------------------------------------------ shared helpers
+struct SmemLayout {
+    int mask_off, rec_off, col_off, gacc_off, touched_off, total;
+};
+
+template <int CD, bool PACK, bool BWD>
+__host__ __device__ inline SmemLayout smem_layout(int B) {
+    constexpr int NV = 7 + CD;
+    constexpr int NG = (NV + 15) / 16;
+    const int nw = B / 32;
+    SmemLayout L;
+    L.mask_off = 16;                                         // after 2 mbarriers
+    L.rec_off = (L.mask_off + nw * nw * 4 + nw * 4 + 127) & ~127;
+    const int colbytes = PACK ? 16 : CD * 4;
+    L.col_off = L.rec_off + 2 * B * (int)sizeof(GeoRec);
+    L.gacc_off = (L.col_off + 2 * B * colbytes + 15) & ~15;
+    L.touched_off = L.gacc_off + (BWD ? B * NG * 16 * 4 : 0);
+    L.total = L.touched_off + (BWD ? B * 4 : 0);
+    return L;
+}
+
+// Conservative pixel-centre bounding box of {d : d^T Q d < 1} for the conic
+// Q = [[cxx, cxy], [cxy, cyy]].  Returns false (no culling) for conics that are
+// not positive definite or so elongated that FP32 rounding of sigma could put a
+// pixel outside the exact ellipse below 1.
+__device__ __forceinline__ bool conic_box(const GeoRec &r, float &ex, float &ey) {
+    const float det = r.cxx * r.cyy - r.cxy * r.cxy;
+    const bool ok = (r.cxx > 0.f) && (r.cyy > 0.f) && (det > 1e-3f * r.cxx * r.cyy);
+    if (!ok) return false;
+    ex = sqrtf(r.cyy / det) * 1.002f + 1e-2f;
+    ey = sqrtf(r.cxx / det) * 1.002f + 1e-2f;
+    return true;
+}
+
+// Issues the bulk copies of batch [bs, bs+cnt) into buffer `buf` (thread 0).
+template <bool PACK>
+__device__ __forceinline__ void issue_batch(const RasterArgs &a, GeoRec *srec, float4 *scol4,
+                                            uint64_t *mbar, int B, int buf, int32_t bs,
+                                            int cnt) {
+    fence_proxy_async_smem();
+    const uint32_t bytes = (uint32_t)cnt * (32u + (PACK ? 16u : 0u));
+    mbar_arrive_expect_tx(&mbar[buf], bytes);
+    bulk_g2s(srec + buf * B, a.recs + bs, (uint32_t)cnt * 32u, &mbar[buf]);
+    if (PACK) bulk_g2s(scol4 + buf * B, a.rcols + bs, (uint32_t)cnt * 16u, &mbar[buf]);
+}
+
+// Per-batch culling masks.  Thread tid describes record tid of the batch;
+// for every warp w of the CTA one ballot gives the 32 bits of this thread's
+// warp in w's mask.  limit[w] bounds the record index for warp w (backward).
+__device__ __forceinline__ void build_masks(const GeoRec &r, bool valid, int idx, int nw,
+                                            int wpr, int tile_x0, int tile_y0, int warp,
+                                            int lane, uint32_t *wmask, const int32_t *limit) {
+    float ex = 0.f, ey = 0.f;
+    const bool boxed = valid && conic_box(r, ex, ey);
+    for (int w = 0; w < nw; ++w) {
+        const float x0 = (float)(tile_x0 + (w % wpr) * 8) + 0.5f;
+        const float y0 = (float)(tile_y0 + (w / wpr) * 4) + 0.5f;
+        bool ov = valid;
+        if (boxed)
+            ov = (r.x - ex <= x0 + 7.f) && (r.x + ex >= x0) && (r.y - ey <= y0 + 3.f) &&
+                 (r.y + ey >= y0);
+        if (limit) ov = ov && (idx <= limit[w]);
+        const uint32_t word = __ballot_sync(0xffffffffu, ov);
+        if (lane == 0) wmask[w * nw + warp] = word;
+    }
+}
+
+// --------------------------------------------------------------- forward
+template <int CD, bool PACK>
+__global__ void __launch_bounds__(1024) raster_fwd_kernel(RasterArgs a) {
+    extern __shared__ __align__(128) unsigned char sm[];
+    const int B = blockDim.x;
+    const int nw = B >> 5;
+    const SmemLayout L = smem_layout<CD, PACK, false>(B);
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(sm);
+    uint32_t *wmask = reinterpret_cast<uint32_t *>(sm + L.mask_off);
+    GeoRec *srec = reinterpret_cast<GeoRec *>(sm + L.rec_off);
+    float4 *scol4 = reinterpret_cast<float4 *>(sm + L.col_off);
+    float *scol = reinterpret_cast<float *>(sm + L.col_off);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int bt = blockIdx.x;
+    const int cam = bt / a.n_tiles;
+    const int tile = bt - cam * a.n_tiles;
+    const int ty = tile / a.TW, tx = tile - ty * a.TW;
+    const int wpr = a.TS >> 3;
+    const int i = ty * a.TS + (warp / wpr) * 4 + (lane >> 3);
+    const int j = tx * a.TS + (warp % wpr) * 8 + (lane & 7);
+    const bool inside = (i < a.H) && (j < a.W);
+    const int64_t pix = ((int64_t)cam * a.H + i) * a.W + j;
+    const float *bg = a.bg ? a.bg + (int64_t)cam * CD : nullptr;
+
+    if (a.masks && !a.masks[bt]) {
+        if (inside) {
+#pragma unroll
+            for (int k = 0; k < CD; ++k) a.out_c[pix * CD + k] = bg ? bg[k] : 0.f;
+            a.out_a[pix] = 0.f;
+            a.last_ids[pix] = 0;
+        }
+        return;
+    }
+
+    int32_t rs = a.offsets[bt];
+    int32_t re = (bt == a.C * a.n_tiles - 1) ? (int32_t)a.n_isects : a.offsets[bt + 1];
+    rs = max(0, min(rs, (int32_t)a.n_isects));
+    re = max(rs, min(re, (int32_t)a.n_isects));
+    const int nb = (re - rs + B - 1) / B;
+
+    const float px = (float)j + 0.5f, py = (float)i + 0.5f;
+    float T = 1.0f;
+    int32_t cur = 0;
+    float acc[CD];
+#pragma unroll
+    for (int k = 0; k < CD; ++k) acc[k] = 0.f;
+    bool done = !inside;
+
+    if (nb > 0) {
+        if (tid == 0) {
+            mbar_init(&mbar[0], 1);
+            mbar_init(&mbar[1], 1);
+            fence_barrier_init();
+        }
+        __syncthreads();
+        int issued = 0, waited = 0;
+        if (tid == 0) {
+            issue_batch<PACK>(a, srec, scol4, mbar, B, 0, rs, min(B, re - rs));
+            issued = 1;
+        }
+        for (int b = 0; b < nb; ++b) {
+            const int32_t bs = rs + b * B;
+            const int cnt = min(B, re - bs);
+            const int buf = b & 1;
+            if (tid == 0 && b + 1 < nb) {
+                const int32_t bn = bs + B;
+                issue_batch<PACK>(a, srec, scol4, mbar, B, buf ^ 1, bn, min(B, re - bn));
+                issued = b + 2;
+            }
+            const bool ok = mbar_wait_bounded(&mbar[buf], (b >> 1) & 1);
+            if (tid == 0 && ok) waited = b + 1;
+            const bool valid = tid < cnt;
+            GeoRec r;
+            if (valid) r = srec[buf * B + tid];
+            build_masks(r, valid, 0, nw, wpr, tx * a.TS, ty * a.TS, warp, lane, wmask, nullptr);
+            if (!PACK && valid) {
+                const float *cp = a.colors + (int64_t)r.gid * CD;
+#pragma unroll
+                for (int k = 0; k < CD; ++k) scol[(buf * B + tid) * CD + k] = cp[k];
+            }
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) atomicOr(a.status, DEV_ERR_WAIT_TIMEOUT);
+                done = true;
+                break;
+            }
+            if (!__all_sync(0xffffffffu, done)) {
+                bool warp_done = false;
+                for (int k = 0; k < nw && !warp_done; ++k) {
+                    uint32_t m = wmask[warp * nw + k];
+                    while (m) {
+                        const int bit = __ffs(m) - 1;
+                        m &= m - 1;
+                        const int t = k * 32 + bit;
+                        const GeoRec q = srec[buf * B + t];
+                        if (!done) {
+                            const float dx = q.x - px, dy = q.y - py;
+                            const float sigma =
+                                (q.cxx * dx * dx + q.cyy * dy * dy) + 2.f * q.cxy * dx * dy;
+                            if (!(sigma < 0.f || sigma >= 1.f)) {
+                                const float alpha =
+                                    fminf(0.999f, q.opac * __powf(1.f - sigma, q.beta));
+                                const float next_T = T * (1.f - alpha);
+                                if (next_T <= 1e-4f) {
+                                    done = true;
+                                } else {
+                                    const float vis = alpha * T;
+                                    if (PACK) {
+                                        const float4 c = scol4[buf * B + t];
+                                        acc[0] += c.x * vis;
+                                        if (CD > 1) acc[1 % CD] += c.y * vis;
+                                        if (CD > 2) acc[2 % CD] += c.z * vis;
+                                        if (CD > 3) acc[3 % CD] += c.w * vis;
+                                    } else {
+#pragma unroll
+                                        for (int k2 = 0; k2 < CD; ++k2)
+                                            acc[k2] += scol[(buf * B + t) * CD + k2] * vis;
+                                    }
+                                    cur = bs + t;
+                                    T = next_T;
+                                }
+                            }
+                        }
+                        if (__all_sync(0xffffffffu, done)) {
+                            warp_done = true;
+                            break;
+                        }
+                    }
+                }
+            }
+            if (__syncthreads_count(done) == B) break;
+        }
+        // make sure no bulk copy still targets this CTA's shared memory
+        if (tid == 0)
+            for (int b = waited; b < issued; ++b)
+                if (!mbar_wait_bounded(&mbar[b & 1], (b >> 1) & 1))
+                    atomicOr(a.status, DEV_ERR_WAIT_TIMEOUT);
+    }
+
+    if (inside) {
+        a.out_a[pix] = 1.0f - T;
+#pragma unroll
+        for (int k = 0; k < CD; ++k) a.out_c[pix * CD + k] = bg ? acc[k] + T * bg[k] : acc[k];
+        a.last_ids[pix] = cur;
+    }
+}
+
+// -------------------------------------------------------------- backward
+template <int CD, bool PACK>
+__global__ void __launch_bounds__(1024) raster_bwd_kernel(RasterArgs a) {
+    constexpr int NV = 7 + CD;
+    constexpr int NG = (NV + 15) / 16;
+    extern __shared__ __align__(128) unsigned char sm[];
+    const int B = blockDim.x;
+    const int nw = B >> 5;
+    const SmemLayout L = smem_layout<CD, PACK, true>(B);
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(sm);
+    uint32_t *wmask = reinterpret_cast<uint32_t *>(sm + L.mask_off);
+    int32_t *wbin = reinterpret_cast<int32_t *>(sm + L.mask_off + nw * nw * 4);
+    GeoRec *srec = reinterpret_cast<GeoRec *>(sm + L.rec_off);
+    float4 *scol4 = reinterpret_cast<float4 *>(sm + L.col_off);
+    float *scol = reinterpret_cast<float *>(sm + L.col_off);
+    float *gacc = reinterpret_cast<float *>(sm + L.gacc_off);
+    int32_t *touched = reinterpret_cast<int32_t *>(sm + L.touched_off);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int bt = blockIdx.x;
+    if (a.masks && !a.masks[bt]) return;
+    const int cam = bt / a.n_tiles;
+    const int tile = bt - cam * a.n_tiles;
+    const int ty = tile / a.TW, tx = tile - ty * a.TW;
+    const int wpr = a.TS >> 3;
+    const int i = ty * a.TS + (warp / wpr) * 4 + (lane >> 3);
+    const int j = tx * a.TS + (warp % wpr) * 8 + (lane & 7);
+    const bool inside = (i < a.H) && (j < a.W);
+    // outside threads read a clamped pixel, like the reference, and never contribute
+    const int64_t pix_in = min((int64_t)i * a.W + j, (int64_t)a.W * a.H - 1);
+    const int64_t pix = (int64_t)cam * a.H * a.W + pix_in;
+    const float *bg = a.bg ? a.bg + (int64_t)cam * CD : nullptr;
+
+    int32_t rs = a.offsets[bt];
+    int32_t re = (bt == a.C * a.n_tiles - 1) ? (int32_t)a.n_isects : a.offsets[bt + 1];
+    rs = max(0, min(rs, (int32_t)a.n_isects));
+    re = max(rs, min(re, (int32_t)a.n_isects));
+
+    const float px = (float)j + 0.5f, py = (float)i + 0.5f;
+    const float T_final = 1.0f - a.render_alphas[pix];
+    float T = T_final;
+    const int32_t bin_final = inside ? a.last_in[pix] : 0;
+    float vrc[CD], buf_c[CD];
+#pragma unroll
+    for (int k = 0; k < CD; ++k) {
+        vrc[k] = a.v_out_c[pix * CD + k];
+        buf_c[k] = 0.f;
+    }
+    const float vra = a.v_out_a[pix];
+    float bgdot = 0.f;
+    if (bg) {
+#pragma unroll
+        for (int k = 0; k < CD; ++k) bgdot += bg[k] * vrc[k];
+    }
+
+    // warp- and block-level bounds on the last contributor index
+    const int32_t wb = __reduce_max_sync(0xffffffffu, inside ? bin_final : INT32_MIN);
+    if (lane == 0) wbin[warp] = wb;
+    for (int t = tid; t < B * NG * 16; t += B) gacc[t] = 0.f;
+    touched[tid] = 0;
+    if (tid == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    int32_t block_bin = INT32_MIN;
+    for (int w = 0; w < nw; ++w) block_bin = max(block_bin, wbin[w]);
+    const int32_t hi_end = max(rs, min(re, block_bin + 1)); // exclusive upper index
+    const int nb = (hi_end - rs + B - 1) / B;
+
+    int issued = 0, waited = 0;
+    if (nb > 0 && tid == 0) {
+        const int32_t lo = max(rs, hi_end - B);
+        issue_batch<PACK>(a, srec, scol4, mbar, B, 0, lo, hi_end - lo);
+        issued = 1;
+    }
+    for (int b = 0; b < nb; ++b) {
+        const int32_t hi = hi_end - b * B;
+        const int32_t lo = max(rs, hi - B);
+        const int cnt = hi - lo;
+        const int buf = b & 1;
+        if (tid == 0 && b + 1 < nb) {
+            const int32_t hn = hi - B;
+            const int32_t ln = max(rs, hn - B);
+            issue_batch<PACK>(a, srec, scol4, mbar, B, buf ^ 1, ln, hn - ln);
+            issued = b + 2;
+        }
+        const bool ok = mbar_wait_bounded(&mbar[buf], (b >> 1) & 1);
+        if (tid == 0 && ok) waited = b + 1;
+        const bool valid = tid < cnt;
+        GeoRec r;
+        int32_t my_gid = 0;
+        if (valid) {
+            r = srec[buf * B + tid];
+            my_gid = r.gid;
+        }
+        build_masks(r, valid, lo + tid, nw, wpr, tx * a.TS, ty * a.TS, warp, lane, wmask, wbin);
+        if (!PACK && valid) {
+            const float *cp = a.colors + (int64_t)my_gid * CD;
+#pragma unroll
+            for (int k = 0; k < CD; ++k) scol[(buf * B + tid) * CD + k] = cp[k];
+        }
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicOr(a.status, DEV_ERR_WAIT_TIMEOUT);
+            break;
+        }
+        for (int k = nw - 1; k >= 0; --k) {
+            uint32_t m = wmask[warp * nw + k];
+            while (m) {
+                const int bit = 31 - __clz(m);
+                m &= ~(1u << bit);
+                const int t = k * 32 + bit;
+                const int32_t idx = lo + t;
+                const GeoRec q = srec[buf * B + t];
+                bool v = inside && (idx <= bin_final);
+                float dx = 0.f, dy = 0.f, sigma = 0.f, vis = 0.f, alpha = 0.f;
+                if (v) {
+                    dx = q.x - px;
+                    dy = q.y - py;
+                    sigma = (q.cxx * dx * dx + q.cyy * dy * dy) + 2.f * q.cxy * dx * dy;
+                    if (sigma < 0.f || sigma >= 1.f) v = false;
+                    vis = __powf(1.f - sigma, q.beta);
+                    alpha = fminf(0.999f, q.opac * vis);
+                }
+                if (!__any_sync(0xffffffffu, v)) continue;
+                float g[NG * 16];
+#pragma unroll
+                for (int u = 0; u < NG * 16; ++u) g[u] = 0.f;
+                if (v) {
+                    float col[CD];
+                    if (PACK) {
+                        const float4 c = scol4[buf * B + t];
+                        col[0] = c.x;
+                        if (CD > 1) col[1 % CD] = c.y;
+                        if (CD > 2) col[2 % CD] = c.z;
+                        if (CD > 3) col[3 % CD] = c.w;
+                    } else {
+#pragma unroll
+                        for (int k2 = 0; k2 < CD; ++k2) col[k2] = scol[(buf * B + t) * CD + k2];
+                    }
+                    const float ra = 1.0f / (1.0f - alpha);
+                    T *= ra;
+                    const float fac = alpha * T;
+                    float v_alpha = 0.f;
+#pragma unroll
+                    for (int k2 = 0; k2 < CD; ++k2) {
+                        g[7 + k2] = fac * vrc[k2];
+                        v_alpha += (col[k2] * T - buf_c[k2] * ra) * vrc[k2];
+                    }
+                    v_alpha += T_final * ra * vra;
+                    if (bg) v_alpha += -T_final * ra * bgdot;
+                    if (q.opac * vis <= 0.999f) {
+                        const float v_sigma =
+                            -v_alpha * q.opac * q.beta * __powf(1.f - sigma, q.beta - 1.f);
+                        g[2] = dx * dx * v_sigma;
+                        g[3] = 2.f * dx * dy * v_sigma;
+                        g[4] = dy * dy * v_sigma;
+                        g[0] = 2.f * v_sigma * (q.cxx * dx + q.cxy * dy);
+                        g[1] = 2.f * v_sigma * (q.cxy * dx + q.cyy * dy);
+                        g[5] = vis * v_alpha;
+                        g[6] = v_alpha * q.opac * __powf(1.f - sigma, q.beta) *
+                               __logf(1.f - sigma);
+                    }
+#pragma unroll
+                    for (int k2 = 0; k2 < CD; ++k2) buf_c[k2] += col[k2] * fac;
+                }
+#pragma unroll
+                for (int grp = 0; grp < NG; ++grp) {
+                    float vv[16];
+#pragma unroll
+                    for (int u = 0; u < 16; ++u) vv[u] = g[grp * 16 + u];
+                    const float tot = warp_transpose_reduce16(vv, lane);
+                    const int vi = grp * 16 + transpose_reduce_index(lane);
+                    if (!(lane & 1) && vi < NV && tot != 0.f)
+                        atomicAdd(&gacc[t * NG * 16 + vi], tot);
+                }
+                if (lane == 0) touched[t] = 1;
+            }
+        }
+        __syncthreads();
+        if (valid && touched[tid]) {
+            const int64_t gg = my_gid;
+            float *ga = gacc + tid * NG * 16;
+#pragma unroll
+            for (int u = 0; u < NV; ++u) {
+                const float val = ga[u];
+                if (val != 0.f) {
+                    float *dst;
+                    if (u < 2) dst = a.v_m2 + 2 * gg + u;
+                    else if (u < 5) dst = a.v_cn + 3 * gg + (u - 2);
+                    else if (u == 5) dst = a.v_op + gg;
+                    else if (u == 6) dst = a.v_be + gg;
+                    else dst = a.v_col + gg * CD + (u - 7);
+                    atomicAdd(dst, val);
+                }
+                ga[u] = 0.f;
+            }
+            touched[tid] = 0;
+        }
+    }
+    if (tid == 0)
+        for (int b = waited; b < issued; ++b)
+            if (!mbar_wait_bounded(&mbar[b & 1], (b >> 1) & 1))
+                atomicOr(a.status, DEV_ERR_WAIT_TIMEOUT);
+}
+
+// ------------------------------------------------------------- host side
+static bool channels_supported(int ch) {
+    switch (ch) {
+    case 1: case 2: case 3: case 4: case 5: case 8: case 9:
+    case 16: case 17: case 32: case 33:
+        return true;
+    default:
+        return false;
+    }
+}
+
+size_t raster_ws_bytes(int64_t T, int ch) {
+    size_t b = 256 + (size_t)T * sizeof(GeoRec);
+    if (ch <= 4) b += (size_t)T * 16;
+    return b;
+}
+
+struct RasterHost {
+    RasterArgs a;
+    int channels;
+    cudaStream_t st;
+};
+
+template <int CD, bool BWD>
+static int launch_raster(RasterArgs &a, int64_t T, const int32_t *fl, const float *m2,
+                         const float *cn, const float *op, const float *be, const float *col,
+                         cudaStream_t st) {
+    constexpr bool PACK = CD <= 4;
+    // pack sorted records
+    if (T > 0) {
+        const int blk = 256;
+        const int64_t nblk = (T + blk - 1) / blk;
+        const unsigned grid = (unsigned)(nblk < 152 * 16 ? nblk : 152 * 16);
+        pack_records_kernel<CD, PACK><<<grid, blk, 0, st>>>(
+            T, a.n_prims, fl, m2, cn, op, be, col, const_cast<GeoRec *>(a.recs),
+            const_cast<float4 *>(a.rcols), a.status);
+        if (int e = check_launch("pack_records")) return e;
+    }
+    const int B = a.TS * a.TS;
+    const SmemLayout L = smem_layout<CD, PACK, BWD>(B);
+    if (L.total > 227 * 1024)
+        return set_error(UBS_ERR_UNSUPPORTED, "raster: tile_size %d with %d channels needs %d B "
+                                              "of shared memory", a.TS, CD, L.total);
+    const unsigned nblocks = (unsigned)((int64_t)a.C * a.n_tiles);
+    if (nblocks == 0) return UBS_OK;
+    if (BWD) {
+        auto k = raster_bwd_kernel<CD, PACK>;
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total) !=
+            cudaSuccess)
+            return check_launch("raster_bwd smem attribute");
+        k<<<nblocks, B, L.total, st>>>(a);
+        return check_launch("raster_bwd");
+    } else {
+        auto k = raster_fwd_kernel<CD, PACK>;
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total) !=
+            cudaSuccess)
+            return check_launch("raster_fwd smem attribute");
+        k<<<nblocks, B, L.total, st>>>(a);
+        return check_launch("raster_fwd");
+    }
+}
+
+template <bool BWD>
+static int dispatch_raster(int ch, RasterArgs &a, int64_t T, const int32_t *fl,
+                           const float *m2, const float *cn, const float *op, const float *be,
+                           const float *col, cudaStream_t st) {
+#define UBS_CASE(n)                                                                       \
+    case n:                                                                               \
+        return launch_raster<n, BWD>(a, T, fl, m2, cn, op, be, col, st);
+    switch (ch) {
+        UBS_CASE(1) UBS_CASE(2) UBS_CASE(3) UBS_CASE(4) UBS_CASE(5) UBS_CASE(8) UBS_CASE(9)
+        UBS_CASE(16) UBS_CASE(17) UBS_CASE(32) UBS_CASE(33)
+    default:
+        return set_error(UBS_ERR_UNSUPPORTED, "raster: %d channels", ch);
+    }
+#undef UBS_CASE
+}
+
+static int validate_raster(int32_t C, int64_t N, int32_t ch, int64_t T, int32_t W, int32_t H,
+                           int32_t ts, int32_t tw, int32_t th, void *ws, size_t ws_bytes) {
+    UBS_REQUIRE(C >= 1 && N >= 0 && W >= 0 && H >= 0, "raster: bad sizes C=%d N=%lld W=%d H=%d",
+                C, (long long)N, W, H);
+    UBS_REQUIRE(T >= 0 && T < (1ll << 31), "raster: n_isects %lld out of range", (long long)T);
+    UBS_REQUIRE((int64_t)C * N < (1ll << 31), "raster: C*N must fit in int32");
+    if (!(ts == 8 || ts == 16 || ts == 24 || ts == 32))
+        return set_error(UBS_ERR_UNSUPPORTED, "raster: tile_size %d (supported 8, 16, 24, 32)",
+                         ts);
+    UBS_REQUIRE((int64_t)tw * ts >= W && (int64_t)th * ts >= H,
+                "raster: tile grid %dx%d of %d px does not cover %dx%d", tw, th, ts, W, H);
+    if (!channels_supported(ch))
+        return set_error(UBS_ERR_UNSUPPORTED, "raster: %d channels (supported 1-5, 8, 9, 16, "
+                                              "17, 32, 33)", ch);
+    UBS_REQUIRE(ws != nullptr && ((uintptr_t)ws & 255) == 0,
+                "raster: workspace must be 256-byte aligned");
+    if (ws_bytes < raster_ws_bytes(T, ch))
+        return set_error(UBS_ERR_OVERFLOW, "raster: workspace %zu B < %zu B needed", ws_bytes,
+                         raster_ws_bytes(T, ch));
+    return UBS_OK;
+}
+
+static void fill_common(RasterArgs &a, int32_t C, int64_t N, int32_t ch, int64_t T, int32_t W,
+                        int32_t H, int32_t ts, int32_t tw, int32_t th, const int32_t *offs,
+                        const float *colors, const float *bg, const uint8_t *masks, void *ws) {
+    a.C = C;
+    a.W = W;
+    a.H = H;
+    a.TS = ts;
+    a.TW = tw;
+    a.TH = th;
+    a.n_tiles = tw * th;
+    a.n_isects = T;
+    a.n_prims = (int64_t)C * N;
+    a.offsets = offs;
+    unsigned char *w = static_cast<unsigned char *>(ws);
+    a.status = reinterpret_cast<uint32_t *>(w);
+    a.recs = reinterpret_cast<const GeoRec *>(w + 256);
+    a.rcols = ch <= 4 ? reinterpret_cast<const float4 *>(w + 256 + T * sizeof(GeoRec)) : nullptr;
+    a.colors = colors;
+    a.bg = bg;
+    a.masks = masks;
+}
+
+} // namespace ubs
+
+using namespace ubs;
+
+extern "C" {
+
+size_t ubs_raster_workspace_bytes(int64_t n_isects, int32_t channels) {
+    return raster_ws_bytes(n_isects < 0 ? 0 : n_isects, channels);
+}
+
+int ubs_raster_fwd(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
+                   const float *means2d, const float *conics, const float *colors,
+                   const float *opacities, const float *betas, const float *backgrounds,
+                   const uint8_t *masks, int32_t width, int32_t height, int32_t tile_size,
+                   int32_t tile_width, int32_t tile_height, const int32_t *isect_offsets,
+                   const int32_t *flatten_ids, float *render_colors, float *render_alphas,
+                   int32_t *last_ids, void *workspace, size_t workspace_bytes, void *stream) {
+    if (int e = validate_raster(C, N, channels, n_isects, width, height, tile_size, tile_width,
+                                tile_height, workspace, workspace_bytes))
+        return e;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    RasterArgs a{};
+    fill_common(a, C, N, channels, n_isects, width, height, tile_size, tile_width, tile_height,
+                isect_offsets, colors, backgrounds, masks, workspace);
+    a.out_c = render_colors;
+    a.out_a = render_alphas;
+    a.last_ids = last_ids;
+    if (cudaMemsetAsync(a.status, 0, 4, st) != cudaSuccess) return check_launch("memset");
+    return dispatch_raster<false>(channels, a, n_isects, flatten_ids, means2d, conics, opacities,
+                                  betas, colors, st);
+}
+
+int ubs_raster_bwd(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
+                   const float *means2d, const float *conics, const float *colors,
+                   const float *opacities, const float *betas, const float *backgrounds,
+                   const uint8_t *masks, int32_t width, int32_t height, int32_t tile_size,
+                   int32_t tile_width, int32_t tile_height, const int32_t *isect_offsets,
+                   const int32_t *flatten_ids, const float *render_alphas,
+                   const int32_t *last_ids, const float *v_render_colors,
+                   const float *v_render_alphas, float *v_means2d, float *v_conics,
+                   float *v_colors, float *v_opacities, float *v_betas, void *workspace,
+                   size_t workspace_bytes, void *stream) {
+    if (int e = validate_raster(C, N, channels, n_isects, width, height, tile_size, tile_width,
+                                tile_height, workspace, workspace_bytes))
+        return e;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int64_t P = (int64_t)C * N;
+    if (cudaMemsetAsync(v_means2d, 0, P * 2 * 4, st) ||
+        cudaMemsetAsync(v_conics, 0, P * 3 * 4, st) ||
+        cudaMemsetAsync(v_colors, 0, P * channels * 4, st) ||
+        cudaMemsetAsync(v_opacities, 0, P * 4, st) || cudaMemsetAsync(v_betas, 0, P * 4, st))
+        return check_launch("raster_bwd memset");
+    if (n_isects == 0) return UBS_OK;
+    RasterArgs a{};
+    fill_common(a, C, N, channels, n_isects, width, height, tile_size, tile_width, tile_height,
+                isect_offsets, colors, backgrounds, masks, workspace);
+    a.render_alphas = render_alphas;
+    a.last_in = last_ids;
+    a.v_out_c = v_render_colors;
+    a.v_out_a = v_render_alphas;
+    a.v_m2 = v_means2d;
+    a.v_cn = v_conics;
+    a.v_col = v_colors;
+    a.v_op = v_opacities;
+    a.v_be = v_betas;
+    if (cudaMemsetAsync(a.status, 0, 4, st) != cudaSuccess) return check_launch("memset");
+    return dispatch_raster<true>(channels, a, n_isects, flatten_ids, means2d, conics, opacities,
+                                 betas, colors, st);
+}
+
+int ubs_raster_status(const void *workspace, uint32_t *status, void *stream) {
+    UBS_REQUIRE(workspace && status, "raster_status: null pointer");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (cudaMemcpyAsync(status, workspace, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return check_launch("raster_status");
+    return UBS_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,129 @@
+// ubs_common.cuh -- shared device/host helpers of the GB300 rasteriser library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/ubs.h"
+
+namespace ubs {
+
+// ------------------------------------------------------------- error state
+// The last error message of the calling host thread (read by ubs_last_error).
+int set_error(int code, const char *fmt, ...);
+int check_launch(const char *what);
+
+#define UBS_REQUIRE(cond, ...)                                                  \
+    do {                                                                        \
+        if (!(cond)) return ::ubs::set_error(UBS_ERR_INVALID, __VA_ARGS__);     \
+    } while (0)
+
+inline unsigned grid_for(int64_t n, int block) {
+    return (unsigned)((n + block - 1) / block);
+}
+
+// Device-side status word: kernels OR error bits into it instead of trapping.
+enum DeviceError : uint32_t {
+    DEV_ERR_WAIT_TIMEOUT = 1u,   // an mbarrier wait ran out of iterations
+    DEV_ERR_NEG_DEPTH = 2u,      // a visible primitive had a negative depth key
+    DEV_ERR_OVERFLOW = 4u,       // an intersection buffer was too small
+};
+
+// ------------------------------------------------------- small device math
+__device__ __forceinline__ float clamp01_eps(float x) {
+    const float maxv = 1.0f - 1.1920928955078125e-07f; // 1 - FLT_EPSILON
+    x = x < 0.0f ? 0.0f : x;
+    return x > maxv ? maxv : x;
+}
+
+// ------------------------------------------ mbarrier + bulk async copy (TMA)
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+__device__ __forceinline__ void fence_barrier_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+// Bulk (non-tensor) async copy global -> shared, completion on the mbarrier.
+// dst, src 16-byte aligned; bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                         uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: gives up after max_iters polls and reports false.  try_wait
+// itself suspends for a hardware-defined interval, so the bound is generous.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity,
+                                                  uint32_t max_iters = (1u << 22)) {
+    for (uint32_t i = 0; i < max_iters; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// -------------------------------------------------- warp transpose-reduce
+// Sums 16 per-lane values over the 32 lanes of a warp with 16 shuffles
+// (instead of 16 x 5).  On return lane L holds the warp total of value
+// index ((L>>4)&1)*8 + ((L>>3)&1)*4 + ((L>>2)&1)*2 + ((L>>1)&1) in v[0];
+// lanes L and L^1 hold the same total.
+__device__ __forceinline__ int transpose_reduce_index(int lane) {
+    return ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 +
+           ((lane >> 1) & 1);
+}
+__device__ __forceinline__ float warp_transpose_reduce16(float (&v)[16], int lane) {
+    const unsigned full = 0xffffffffu;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const bool hi = lane & 16;
+        const float send = hi ? v[i] : v[i + 8];
+        const float keep = hi ? v[i + 8] : v[i];
+        v[i] = keep + __shfl_xor_sync(full, send, 16);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const bool hi = lane & 8;
+        const float send = hi ? v[i] : v[i + 4];
+        const float keep = hi ? v[i + 4] : v[i];
+        v[i] = keep + __shfl_xor_sync(full, send, 8);
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const bool hi = lane & 4;
+        const float send = hi ? v[i] : v[i + 2];
+        const float keep = hi ? v[i + 2] : v[i];
+        v[i] = keep + __shfl_xor_sync(full, send, 4);
+    }
+    {
+        const bool hi = lane & 2;
+        const float send = hi ? v[0] : v[1];
+        const float keep = hi ? v[1] : v[0];
+        v[0] = keep + __shfl_xor_sync(full, send, 2);
+    }
+    v[0] += __shfl_xor_sync(full, v[0], 1);
+    return v[0];
+}
+
+} // namespace ubs

@@ -1,0 +1,113 @@
+"""ctypes binding of the C ABI declared in include/ubs.h.
+
+The library is the only compute path: there is no CPU or PyTorch fallback.
+If it cannot be built or loaded, or a CUDA device is missing, calls raise.
+"""
+import ctypes
+import os
+import threading
+
+import torch
+
+from . import build as _build
+
+_P = ctypes.c_void_p
+_I32 = ctypes.c_int32
+_I64 = ctypes.c_int64
+_F = ctypes.c_float
+_SZ = ctypes.c_size_t
+_U32P = ctypes.POINTER(ctypes.c_uint32)
+_I64P = ctypes.POINTER(ctypes.c_int64)
+_INT = ctypes.c_int
+
+# name -> (argtypes, restype); keep in step with include/ubs.h
+SIGNATURES = {
+    "ubs_last_error": ([], ctypes.c_char_p),
+    "ubs_abi_version": ([], _INT),
+    "ubs_l_triangle_to_rotmat_fwd": ([_I64, _P, _I64, _P, _P], _INT),
+    "ubs_l_triangle_to_rotmat_bwd": ([_I64, _P, _P, _P], _INT),
+    "ubs_rot_scale_l_triangle_to_covar_fwd": ([_I64, _I32, _P, _P, _P, _P, _P, _I32, _I32, _P, _P],
+                                              _INT),
+    "ubs_rot_scale_l_triangle_to_covar_bwd": ([_I64, _I32, _P, _P, _P, _P, _P, _I32, _I32, _P,
+                                               _P, _P, _P, _P], _INT),
+    "ubs_cond_fwd": ([_I64, _I32] + [_P] * 8 + [_P], _INT),
+    "ubs_cond_bwd": ([_I64, _I32] + [_P] * 12 + [_I32, _P], _INT),
+    "ubs_projection_fwd": ([_I32, _I64, _P, _P, _I32, _P, _P, _P, _P, _I32, _I32, _F, _F, _F, _F,
+                            _P, _P, _P, _P, _P, _P], _INT),
+    "ubs_projection_bwd": ([_I32, _I64, _P, _P, _I32, _P, _P, _P, _P, _I32, _I32, _F]
+                           + [_P] * 7 + [_P] * 5 + [_P], _INT),
+    "ubs_isect_count_workspace_bytes": ([_I32, _I64, _I32], _SZ),
+    "ubs_isect_sort_workspace_bytes": ([_I32, _I64, _I32, _I64], _SZ),
+    "ubs_isect_count": ([_I32, _I64, _P, _P, _P, _I32, _I32, _I32, _P, _P, _I64P, _P, _SZ, _P],
+                        _INT),
+    "ubs_isect_emit": ([_I32, _I64, _P, _P, _P, _I32, _I32, _I32, _P, _P, _I64, _I32, _P, _P, _P,
+                        _SZ, _P], _INT),
+    "ubs_isect_offset_encode": ([_I64, _P, _I32, _I32, _I32, _P, _P], _INT),
+    "ubs_raster_workspace_bytes": ([_I64, _I32], _SZ),
+    "ubs_raster_fwd": ([_I32, _I64, _I32, _I64] + [_P] * 7 + [_I32] * 5 + [_P] * 5 + [_P, _SZ, _P],
+                       _INT),
+    "ubs_raster_bwd": ([_I32, _I64, _I32, _I64] + [_P] * 7 + [_I32] * 5 + [_P] * 2 + [_P] * 4
+                       + [_P] * 5 + [_P, _SZ, _P], _INT),
+    "ubs_raster_status": ([_P, _U32P, _P], _INT),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib():
+    """Load (building first if needed) the native library."""
+    global _lib
+    if _lib is None:
+        with _lock:
+            if _lib is None:
+                path = _build.build()
+                L = ctypes.CDLL(path)
+                for name, (argt, rest) in SIGNATURES.items():
+                    fn = getattr(L, name)
+                    fn.argtypes = argt
+                    fn.restype = rest
+                _lib = L
+    return _lib
+
+
+def library_path():
+    return _build.LIB_PATH
+
+
+def last_error():
+    return lib().ubs_last_error().decode(errors="replace")
+
+
+def call(name, *args):
+    """Call an int-returning entry point and raise on a non-zero status."""
+    rc = getattr(lib(), name)(*args)
+    if rc != 0:
+        raise RuntimeError("%s failed (%d): %s" % (name, rc, last_error()))
+    return rc
+
+
+def query(name, *args):
+    return getattr(lib(), name)(*args)
+
+
+def ptr(t, dtype=None):
+    """Device pointer of a contiguous CUDA tensor (None passes NULL)."""
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor, got device %s" % t.device)
+    if not t.is_contiguous():
+        raise ValueError("expected a contiguous tensor")
+    if dtype is not None and t.dtype != dtype:
+        raise TypeError("expected dtype %s, got %s" % (dtype, t.dtype))
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def stream(device=None):
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def workspace(nbytes, device):
+    """Caller-owned scratch memory (the caching allocator aligns to 512 bytes)."""
+    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
