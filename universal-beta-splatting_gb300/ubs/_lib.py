@@ -79,12 +79,41 @@ def last_error():
     return lib().ubs_last_error().decode(errors="replace")
 
 
+_timing = None  # list of (name, start_event, end_event) while timing is on
+
+
 def call(name, *args):
     """Call an int-returning entry point and raise on a non-zero status."""
-    rc = getattr(lib(), name)(*args)
+    if _timing is not None:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        rc = getattr(lib(), name)(*args)
+        e1.record()
+        _timing.append((name, e0, e1))
+    else:
+        rc = getattr(lib(), name)(*args)
     if rc != 0:
         raise RuntimeError("%s failed (%d): %s" % (name, rc, last_error()))
     return rc
+
+
+def start_timing():
+    """Record CUDA events (on the current stream) around every entry-point call."""
+    global _timing
+    _timing = []
+
+
+def stop_timing():
+    """Stop recording; returns {entry point: (calls, total ms)}."""
+    global _timing
+    rec, _timing = _timing or [], None
+    torch.cuda.synchronize()
+    out = {}
+    for name, e0, e1 in rec:
+        n, t = out.get(name, (0, 0.0))
+        out[name] = (n + 1, t + e0.elapsed_time(e1))
+    return out
 
 
 def query(name, *args):
