@@ -1,0 +1,512 @@
+#!/usr/bin/env python
+"""Headline benchmark of the GB300 Universal Beta Splatting rasteriser.
+
+Workload (the reference's plain GPU configuration): 1,000,000 6-D Beta
+primitives (xyz uniform in [-2,2]^3, spatial scales exp(N(-4,0.5)), angular
+scales ~1, rest lower-triangle N(0,0.1), angular raw betas N(0,0.5), spatial raw
+beta N(0,0.3), opacity logits N(0,1), RGB uniform), one 1920x1080 pinhole camera
+(fx=fy=1500) on a radius-4 orbit, 16x16 tiles.  One step = forward render through
+the reference's call sequence (activations, rotation, covariance, conditioning,
+projection, intersection + sort, blend), an L1 loss against a random target and
+the backward pass to all raw parameters.  Data are seeded synthetic tensors with
+the benchmark's distributions (the reference's datasets are not available).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference path on the host CPU (the C++ oracle port
+of every step; the reference itself has no CPU blend).  For N > 1 (torchrun)
+each rank renders an independent replica (the path does not shard).
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "universal-beta-splatting_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+import torch  # noqa: E402
+
+METRIC = "render FPS and train it/s at 1M prims 1080p; serving p50/p99 ms vs plain form"
+N_PRIMS, DIM, WIDTH, HEIGHT, FOCAL, TILE = 1_000_000, 6, 1920, 1080, 1500.0, 16
+# FP32 operations (FMA = 2) per contributing (pixel, primitive) pair in the
+# reference's per-pair arithmetic (rasterize_to_pixels_fwd.cu:140-171,
+# rasterize_to_pixels_bwd.cu:170-247); rejected pairs are not counted.
+FWD_FLOP_PER_PAIR = 28
+BWD_FLOP_PER_PAIR = 77
+WORKLOAD = ("1M 6-D Beta primitives, 1920x1080 (fx=fy=1500), radius-4 orbit camera, 16x16 tiles; "
+            "forward + L1 loss + backward to all raw parameters, one view per step")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n-prims", type=int, default=N_PRIMS)
+    ap.add_argument("--no-ref-gpu", action="store_true", help="skip timing the reference kernels")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------- utilities
+class ClockSampler:
+    """nvidia-smi clock / throttle samples every 200 ms while running."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.rows = []
+        self.proc = None
+        self.marks = {}
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append((time.time(), parts))
+
+    def mark(self, name):
+        self.marks[name] = time.time()
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def summary(self, t0, t1):
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        dev_index = None
+        rows = [r for r in self.rows]
+        if rows:
+            dev_index = min(r[1][0] for r in rows)
+            rows = [r for r in rows if r[1][0] == dev_index]
+        inside = [r for r in rows if t0 <= r[0] <= t1]
+        used = inside if len(inside) >= 3 else rows
+        if not used:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        sm = [num(r[1][1]) for r in used if num(r[1][1]) is not None]
+        mx = [num(r[1][2]) for r in used if num(r[1][2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in used for k in range(4)
+                          if r[1][5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(used), "window": "timed region" if used is inside else "run"}
+
+
+def l2_flush_buffer(dev):
+    return torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+
+# ------------------------------------------------------------- GPU (ours)
+def make_problem(n_prims, seed, dev):
+    from ubs import scene as S
+    p = S.synthetic_params(n_prims, DIM, seed=seed, xyz_range=2.0, device=dev)
+    for v in p.values():
+        v.requires_grad_(True)
+    cam = S.orbit_view(seed, 4.0, WIDTH, HEIGHT, FOCAL, FOCAL, device=dev)
+    ri, rj = S.rest_indices(DIM, dev)
+    bg = torch.zeros(3, device=dev)
+    target = torch.rand(3, HEIGHT, WIDTH, generator=torch.Generator().manual_seed(seed + 7)).to(dev)
+    return p, cam, ri, rj, bg, target
+
+
+def gpu_step(p, cam, ri, rj, bg, target):
+    from ubs import scene as S
+    for v in p.values():
+        v.grad = None
+    img, _, meta = S.render_view(p, cam, bg, ri, rj, tile_size=TILE)
+    loss = (img - target).abs().mean()
+    loss.backward()
+    return loss, meta
+
+
+def time_steps(fn, K, dev, flush):
+    """Per-step CUDA-event time (ms), L2 flushed before every step (untimed)."""
+    total = 0.0
+    for k in range(K):
+        flush.fill_(float(k))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        total += e0.elapsed_time(e1)
+    return total / K
+
+
+def fp32_peak(dev):
+    from ubs import _lib as L
+    import ctypes
+    ws = L.workspace(L.query("ubs_fp32_probe_workspace_bytes"), dev)
+    flops = ctypes.c_double(0)
+    best = 0.0
+    for it in (2000, 2000, 2000):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        L.call("ubs_fp32_probe", it, L.ptr(ws), ws.numel(), ctypes.byref(flops), L.stream(dev))
+        e1.record()
+        e1.synchronize()
+        best = max(best, flops.value / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    return best
+
+
+def count_pairs(p, cam, ri, rj, bg, dev):
+    """Contributing (pixel, primitive) pairs of one forward (device counter)."""
+    import ctypes
+    from gsplat.cuda import _wrapper as Wr
+    from ubs import _lib as L
+    from ubs import scene as S
+    with torch.no_grad():
+        _, _, meta = S.render_view(p, cam, bg, ri, rj, tile_size=TILE)
+        m2, cn = meta["means2d"], meta["conics"]
+        op, be = meta["opacities"].contiguous(), meta["betas"].contiguous()
+        fl, offs = meta["flatten_ids"], meta["isect_offsets"]
+        C, N = op.shape
+        T = fl.numel()
+        colors = p["rgb"].detach().expand(1, -1, -1).contiguous()
+        ws = L.workspace(L.query("ubs_raster_workspace_bytes", T, 3), dev)
+        oc = torch.empty(1, HEIGHT, WIDTH, 3, device=dev)
+        oa = torch.empty(1, HEIGHT, WIDTH, 1, device=dev)
+        li = torch.empty(1, HEIGHT, WIDTH, dtype=torch.int32, device=dev)
+        st = L.stream(dev)
+        L.call("ubs_raster_pack", C, N, 3, T, L.ptr(fl), L.ptr(m2), L.ptr(cn), L.ptr(op),
+               L.ptr(be), L.ptr(colors), L.ptr(ws), ws.numel(), st)
+        L.call("ubs_raster_fwd_packed", C, N, 3, T, L.ptr(colors), L.ptr(bg.view(1, 3)), None,
+               WIDTH, HEIGHT, TILE, meta["tile_width"], meta["tile_height"], L.ptr(offs),
+               L.ptr(oc), L.ptr(oa), L.ptr(li), 1, L.ptr(ws), ws.numel(), st)
+        status = ctypes.c_uint32(0)
+        pairs = ctypes.c_uint64(0)
+        L.call("ubs_raster_status", L.ptr(ws), ctypes.byref(status), ctypes.byref(pairs), st)
+        del Wr
+        return int(pairs.value), int(T), int((meta["radii"] > 0).sum())
+
+
+def read_profile_traffic(kernel):
+    """DRAM bytes per launch from a committed ncu summary (profiles/), if any."""
+    path = os.path.join(ROOT, "profiles", kernel + "_1M_1080p.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+# ------------------------------------------------------- CPU (oracle port)
+def cpu_problem(n_prims, seed):
+    from ubs import scene as S
+    p = {k: v.numpy().astype(np.float32) for k, v in
+         S.synthetic_params(n_prims, DIM, seed=seed, xyz_range=2.0, device="cpu").items()}
+    cam = S.orbit_view(seed, 4.0, WIDTH, HEIGHT, FOCAL, FOCAL, device="cpu")
+    target = torch.rand(3, HEIGHT, WIDTH, generator=torch.Generator().manual_seed(seed + 7)).numpy()
+    ri, rj = S.rest_indices(DIM)
+    return p, cam, ri.numpy(), rj.numpy(), target
+
+
+def cpu_step(p, cam, ri, rj, target, row_step=1):
+    """One forward + L1 + backward of the reference path on the host CPU, every
+    stage run by the C++ oracle (OpenMP over primitives / tiles).  With
+    row_step > 1 the two blend stages run on every row_step-th tile row only.
+    Returns (loss, n_isects, seconds in per-primitive stages, seconds in blend)."""
+    import oracle as orc
+    t_start = time.perf_counter()
+    f32 = np.float32
+    sp = np.log1p(np.exp(-np.abs(p["scale"]))) + np.maximum(p["scale"], 0)
+    beta = (4.0 * np.exp(p["beta"])).astype(f32)
+    opac = (1.0 / (1.0 + np.exp(-p["opacity"]))).astype(f32)
+    vm = cam.viewmat.numpy()[None].astype(f32)
+    K = cam.K.numpy()[None].astype(f32)
+    center = cam.center.numpy().astype(f32)
+    vd = p["xyz"] - center[None]
+    q = (vd / np.linalg.norm(vd, axis=-1, keepdims=True)).astype(f32)
+    R = orc.l_triangle_to_rotmat(p["l_triangle"])
+    cov = orc.rot_scale_l_triangle_to_covar(R, sp, p["l_triangle"], ri, rj)
+    m_nd = np.concatenate([p["xyz"], p["mean"]], 1)
+    om, oV, oo = orc.cond_mean_convariance_opacity(m_nd, cov, opac, beta[:, 1:], q)
+    iu = ([0, 0, 0, 1, 1, 2], [0, 1, 2, 1, 2, 2])
+    c6 = oV[:, iu[0], iu[1]]
+    radii, m2, d, cn, _ = orc.fully_fused_projection(om, c6, None, None, vm, K, WIDTH, HEIGHT)
+    tw, th = math.ceil(WIDTH / TILE), math.ceil(HEIGHT / TILE)
+    _, ids, fl = orc.isect_tiles(m2, radii, d, TILE, tw, th)
+    offs = orc.isect_offset_encode(ids, 1, tw, th)
+    colors = p["rgb"][None]
+    op, be = oo.reshape(1, -1), beta[:, 0].reshape(1, -1)
+    bg = np.zeros((1, 3), f32)
+    t_b0 = time.perf_counter()
+    oc, oa, li = orc.rasterize_to_pixels(m2, cn, colors, op, be, WIDTH, HEIGHT, TILE, offs, fl,
+                                         backgrounds=bg, row_step=row_step)
+    t_blend = time.perf_counter() - t_b0
+    img = oc[0].transpose(2, 0, 1)
+    diff = img - target
+    loss = float(np.abs(diff).mean())
+    v_oc = (np.sign(diff) / diff.size).astype(f32).transpose(1, 2, 0)[None]
+    t_b1 = time.perf_counter()
+    vm2, vcn, vcol, vo, vb = orc.rasterize_to_pixels_bwd(
+        m2, cn, colors, op, be, WIDTH, HEIGHT, TILE, offs, fl, oa, li, v_oc, np.zeros_like(oa),
+        backgrounds=bg, row_step=row_step)
+    t_blend += time.perf_counter() - t_b1
+    vmeans, vc6, _, _, _ = orc.fully_fused_projection_bwd(
+        om, c6, None, None, vm, K, WIDTH, HEIGHT, 0.3, radii, cn, None, vm2, None, vcn)
+    v_oV = np.zeros_like(oV)
+    for k, (i, j) in enumerate(zip(*iu)):
+        v_oV[:, i, j] = vc6[:, k]
+    gm, gV, go, gb = orc.cond_mean_convariance_opacity_bwd(m_nd, cov, opac, beta[:, 1:], q,
+                                                           vmeans, v_oV, vo.reshape(-1, 1))
+    vr, vs, vl = orc.rot_scale_l_triangle_to_covar_bwd(R, sp, p["l_triangle"], ri, rj, gV)
+    vl[:, :3] += orc.l_triangle_to_rotmat_bwd(vr)
+    total = time.perf_counter() - t_start
+    return loss, len(ids), total - t_blend, t_blend
+
+
+CPU_ROW_STEP = 8  # the CPU sample blends every 8th tile row (68 rows -> 9)
+
+
+def run_cpu(steps, warmup, n_prims):
+    """Bounded CPU sample of the full workload: all per-primitive stages (all
+    primitives) plus the forward and backward blend of every 8th tile row; the
+    blend time is scaled by 8 to a full frame."""
+    import oracle as orc
+    p, cam, ri, rj, target = cpu_problem(n_prims, 0)
+    for _ in range(warmup):
+        cpu_step(p, cam, ri, rj, target, CPU_ROW_STEP)
+    t_prim = t_blend = 0.0
+    for _ in range(steps):
+        _, _, a, b = cpu_step(p, cam, ri, rj, target, CPU_ROW_STEP)
+        t_prim += a
+        t_blend += b
+    n_rows = math.ceil(HEIGHT / TILE)
+    frac = math.ceil(n_rows / CPU_ROW_STEP) / n_rows
+    dt = (t_prim + t_blend / frac) / steps
+    return {"value": 1.0 / dt, "unit": "it/s", "ms_per_step": dt * 1e3,
+            "cores": orc.num_threads(), "kind": "port",
+            "sample": "all %d primitives, full per-primitive work, blend forward+backward on "
+                      "every %dth of the %d tile rows; blend time scaled by %.3f to a full "
+                      "1920x1080 frame (C++ oracle port, OpenMP)" % (
+                          n_prims, CPU_ROW_STEP, n_rows, 1 / frac)}
+
+
+# ------------------------------------------------------------------- main
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+
+    if args.impl == "reference":
+        # CPU reference arm: rank 0 only
+        if rank == 0:
+            steps, warmup = args.steps, args.warmup
+            # each step is a bounded sample; keep the whole run within minutes
+            r = run_cpu(steps, warmup, args.n_prims)
+            line = {"metric": METRIC, "value": r["value"], "unit": "it/s", "impl": "reference",
+                    "n_gpus": args.gpus, "steps": steps, "warmup": warmup,
+                    "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+                    "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                    "data": "synthetic (seeded, benchmark distributions)",
+                    "config": {"workload": WORKLOAD, "n_prims": args.n_prims, "dim": DIM,
+                               "width": WIDTH, "height": HEIGHT, "tile_size": TILE,
+                               "device": "host CPU"},
+                    "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                    "e2e": {"value": r["value"], "unit": "it/s", "h2d_bytes_per_step": 0,
+                            "d2h_bytes_per_step": 0}}
+            print(json.dumps(line), flush=True)
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    from ubs import _lib as L
+    L.lib()
+    p, cam, ri, rj, bg, target = make_problem(args.n_prims, rank, dev)
+    flush = l2_flush_buffer(dev)
+    clocks = ClockSampler()
+    clocks.start()
+    step = lambda: gpu_step(p, cam, ri, rj, bg, target)  # noqa: E731
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = L.query("ubs_launch_count")
+    clocks.mark("t0")
+    t_wall = time.perf_counter()
+    ms = time_steps(step, args.steps, dev, flush)
+    wall = time.perf_counter() - t_wall
+    clocks.mark("t1")
+    launches = (L.query("ubs_launch_count") - launches0) // max(1, args.steps)
+    torch.cuda.synchronize()
+    ms_max = ms
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+        dist.barrier()
+    value = world * 1000.0 / ms_max
+
+    # end to end: parameters and target from pinned host memory every step,
+    # the loss read back
+    host = {k: v.detach().cpu().pin_memory() for k, v in p.items()}
+    host_target = target.cpu().pin_memory()
+    h2d = sum(v.numel() * 4 for v in host.values()) + host_target.numel() * 4
+    loss_host = torch.empty(1, pin_memory=True)
+
+    def e2e_step():
+        with torch.no_grad():
+            for k, v in p.items():
+                v.copy_(host[k], non_blocking=True)
+            target.copy_(host_target, non_blocking=True)
+        loss, _ = gpu_step(p, cam, ri, rj, bg, target)
+        loss_host.copy_(loss.detach().view(1), non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    e2e_ms = time_steps(e2e_step, args.steps, dev, flush)
+    e2e_val = world * 1000.0 / e2e_ms
+    clocks.stop()
+
+    # per-entry-point times (CUDA events on the launching stream)
+    K2 = max(5, min(args.steps, 20))
+    L.start_timing()
+    for _ in range(K2):
+        step()
+    stages = {k: t / K2 for k, (n, t) in L.stop_timing().items()}
+    pairs, n_isects, n_visible = count_pairs(p, cam, ri, rj, bg, dev)
+    peak_fp32 = fp32_peak(dev)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    dominant = max(stages, key=stages.get)
+    dom_ms = stages[dominant]
+    flop_pp = BWD_FLOP_PER_PAIR if "bwd" in dominant else FWD_FLOP_PER_PAIR
+    achieved = pairs * flop_pp / (dom_ms * 1e-3) / 1e12
+    roofline = {
+        "kernel": dominant, "bound": "fp32",
+        "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s",
+        "frac": achieved / peak_fp32 if peak_fp32 else None,
+        "traffic": read_profile_traffic(dominant),
+        "algorithmic_work": "%d contributing pairs x %d FP32 ops" % (pairs, flop_pp),
+        "peak_source": "FP32 FMA probe kernel timed in this run (MEASURED_PEAKS.json has HBM "
+                       "%s GB/s and bf16 only)" % peaks.get("hbm_gbs", "n/a"),
+        "launch_ms": dom_ms,
+    }
+
+    # the reference's own kernels, plain one-view-per-launch path, same GPU
+    ref_gpu = None
+    if not args.no_ref_gpu and rank == 0:
+        try:
+            import ref_gpu as RG
+            if RG.available():
+                rp = RG.RefPipeline()
+
+                def ref_step():
+                    for v in p.values():
+                        v.grad = None
+                    img, _, _ = rp.render_view(p, cam.viewmat, cam.K, WIDTH, HEIGHT, cam.center,
+                                               bg, ri, rj, tile_size=TILE)
+                    (img - target).abs().mean().backward()
+
+                for _ in range(3):
+                    ref_step()
+                r_ms = time_steps(ref_step, max(5, min(args.steps, 20)), dev, flush)
+                ref_gpu = {"value": 1000.0 / r_ms, "unit": "it/s", "ms_per_step": r_ms,
+                           "what": "the reference's CUDA kernels (built from its sources for "
+                                   "sm_103) in its plain call sequence on this GPU; intersections "
+                                   "sorted with torch.sort in place of its cub sort"}
+        except Exception as e:  # noqa: BLE001
+            ref_gpu = {"error": str(e)[:200]}
+
+    cpu = None
+    if not args.no_cpu and rank == 0 and world == 1:
+        try:
+            r = run_cpu(1, 0, args.n_prims)
+            cpu = {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        except Exception as e:  # noqa: BLE001
+            cpu = {"error": str(e)[:200]}
+
+    # render-only frames/s (forward, no grad)
+    def fwd_only():
+        from ubs import scene as S
+        with torch.no_grad():
+            S.render_view(p, cam, bg, ri, rj, tile_size=TILE)
+    fwd_ms = time_steps(fwd_only, max(5, min(args.steps, 20)), dev, flush)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "it/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded, benchmark distributions; reference datasets absent)",
+            "config": {"workload": WORKLOAD, "n_prims": args.n_prims, "dim": DIM,
+                       "width": WIDTH, "height": HEIGHT, "tile_size": TILE,
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "256 MB buffer written before every timed step (untimed); "
+                             "per-step CUDA events",
+                       "path": "drop-in operators (gsplat.rendering.rasterization call sequence)"},
+            "render_fps": 1000.0 / fwd_ms,
+            "e2e": {"value": e2e_val, "unit": "it/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": 4},
+            "gpu_launches": int(launches) * args.steps,
+            "launches_per_step": int(launches),
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "ref_gpu": ref_gpu,
+            "clocks": clocks.summary(clocks.marks.get("t0", 0), clocks.marks.get("t1", 0)),
+            "stages_ms": {k: round(v, 4) for k, v in sorted(stages.items(), key=lambda x: -x[1])},
+            "isects": n_isects, "visible": n_visible, "pairs": pairs,
+            "wall_s_timed": wall,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

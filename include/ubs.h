@@ -39,6 +39,16 @@ extern "C" {
 const char *ubs_last_error(void);
 /* ABI version of this library (bumped on any signature change). */
 int ubs_abi_version(void);
+/* Number of kernels this library has launched in the process (no reference
+ * counterpart; used to report launches per benchmark step). */
+unsigned long long ubs_launch_count(void);
+/* FP32 FMA issue-rate probe (no reference counterpart): 8 CTAs of 256 threads
+ * per SM run independent FMA chains; *flops receives the launch's FP32 operation
+ * count so that the caller's event timing gives the measured FP32 peak used as
+ * the blend kernels' roofline denominator.  Workspace: one float per thread. */
+size_t ubs_fp32_probe_workspace_bytes(void);
+int ubs_fp32_probe(int32_t iters, void *workspace, size_t workspace_bytes, double *flops,
+                   void *stream);
 
 /* ------------------------------------------------------------------ a2 ---
  * R = I + A(a01, a02, a12): submodules/gsplat/cuda/_wrapper.py:34
@@ -150,11 +160,16 @@ int ubs_isect_offset_encode(int64_t n_isects, const int64_t *isect_ids, int32_t 
  * [C,N], backgrounds [C,channels] or NULL, masks [C,tile_height,tile_width]
  * uint8 or NULL, isect_offsets [C,tile_height,tile_width], flatten_ids
  * [n_isects].  Forward outputs: render_colors [C,H,W,channels], render_alphas
- * [C,H,W], last_ids [C,H,W] int32.  Backward outputs (overwritten):
- * v_means2d, v_conics, v_colors, v_opacities, v_betas; the background
- * gradient is left to the caller, as in the reference.
- * channels in [1, 33]; tile_size in {8, 16, 24, 32}.
- * Workspace: ubs_raster_workspace_bytes(n_isects, channels). */
+ * [C,H,W], last_ids [C,H,W] int32 (index of the last contributing sorted
+ * intersection).  Backward outputs (overwritten): v_means2d, v_conics,
+ * v_colors, v_opacities, v_betas; the background gradient is left to the
+ * caller, as in the reference.  channels in {1-5, 8, 9, 16, 17, 32, 33};
+ * tile_size in {8, 16, 24, 32}.  Workspace: ubs_raster_workspace_bytes().
+ *
+ * ubs_raster_fwd / _bwd = ubs_raster_pack (gather one record per sorted
+ * intersection into the workspace) + ubs_raster_fwd_packed / _bwd_packed (the
+ * blend kernels, which read only the packed records and `colors` for more than
+ * 4 channels).  A packed workspace may serve one forward and its backward. */
 size_t ubs_raster_workspace_bytes(int64_t n_isects, int32_t channels);
 int ubs_raster_fwd(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
                    const float *means2d, const float *conics, const float *colors,
@@ -173,11 +188,35 @@ int ubs_raster_bwd(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
                    const float *v_render_alphas, float *v_means2d, float *v_conics,
                    float *v_colors, float *v_opacities, float *v_betas, void *workspace,
                    size_t workspace_bytes, void *stream);
+int ubs_raster_pack(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
+                    const int32_t *flatten_ids, const float *means2d, const float *conics,
+                    const float *opacities, const float *betas, const float *colors,
+                    void *workspace, size_t workspace_bytes, void *stream);
+/* count_pairs != 0 also counts contributing (pixel, intersection) pairs into
+ * the workspace header (read with ubs_raster_status). */
+int ubs_raster_fwd_packed(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
+                          const float *colors, const float *backgrounds, const uint8_t *masks,
+                          int32_t width, int32_t height, int32_t tile_size, int32_t tile_width,
+                          int32_t tile_height, const int32_t *isect_offsets,
+                          float *render_colors, float *render_alphas, int32_t *last_ids,
+                          int32_t count_pairs, void *workspace, size_t workspace_bytes,
+                          void *stream);
+/* zero_outputs == 0 leaves the gradient buffers as given (caller zeroed them). */
+int ubs_raster_bwd_packed(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
+                          const float *colors, const float *backgrounds, const uint8_t *masks,
+                          int32_t width, int32_t height, int32_t tile_size, int32_t tile_width,
+                          int32_t tile_height, const int32_t *isect_offsets,
+                          const float *render_alphas, const int32_t *last_ids,
+                          const float *v_render_colors, const float *v_render_alphas,
+                          float *v_means2d, float *v_conics, float *v_colors, float *v_opacities,
+                          float *v_betas, int32_t zero_outputs, void *workspace,
+                          size_t workspace_bytes, void *stream);
 
-/* Device status word of the last raster call on `workspace` (0 = clean);
- * synchronises the stream.  Bits: 1 wait timeout, 2 negative depth,
- * 4 overflow. */
-int ubs_raster_status(const void *workspace, uint32_t *status, void *stream);
+/* Device status word (bits: 1 wait timeout, 2 negative depth, 4 overflow,
+ * 8 bad flatten index) and the contributing-pair count of the last packed
+ * blend on `workspace` (pair_count may be NULL); synchronises the stream. */
+int ubs_raster_status(const void *workspace, uint32_t *status, uint64_t *pair_count,
+                      void *stream);
 
 #ifdef __cplusplus
 }

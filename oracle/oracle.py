@@ -37,9 +37,9 @@ def lib():
                                          + [_P] * 5)
             g("project_bwd").argtypes = ([_I, _I64] + [_P] * 6 + [_I, _I, ft] + [_P] * 12)
             g("raster_fwd").argtypes = ([_I, _I64, _I, _I64] + [_P] * 7
-                                        + [_I, _I, _I, _I, _I] + [_P] * 5)
+                                        + [_I, _I, _I, _I, _I] + [_P] * 5 + [_I])
             g("raster_bwd").argtypes = ([_I, _I64, _I, _I64] + [_P] * 7
-                                        + [_I, _I, _I, _I, _I] + [_P] * 11)
+                                        + [_I, _I, _I, _I, _I] + [_P] * 11 + [_I])
         _lib.ubso_isect_count.argtypes = [_I, _I64, _P, _P, _U32, _U32, _U32, _P]
         _lib.ubso_isect_count.restype = _I64
         _lib.ubso_isect_emit_sort.argtypes = [_I, _I64, _P, _P, _P, _U32, _U32, _U32, _P,
@@ -216,7 +216,8 @@ def isect_offset_encode(isect_ids, n_cameras, tile_width, tile_height):
 
 def rasterize_to_pixels(means2d, conics, colors, opacities, betas, width, height, tile_size,
                         isect_offsets, flatten_ids, backgrounds=None, masks=None,
-                        dtype=np.float32):
+                        dtype=np.float32, row_step=1):
+    """row_step > 1 blends only every row_step-th tile row (a timing sample)."""
     means2d, conics, colors = _c(means2d, dtype), _c(conics, dtype), _c(colors, dtype)
     opacities, betas = _c(opacities, dtype), _c(betas, dtype)
     offs = _c(isect_offsets, np.int32)
@@ -230,13 +231,15 @@ def rasterize_to_pixels(means2d, conics, colors, opacities, betas, width, height
     li = np.zeros((C, height, width), np.int32)
     _fn("raster_fwd", dtype)(C, N, cd, len(fl), _p(means2d), _p(conics), _p(colors),
                              _p(opacities), _p(betas), _p(bg), _p(mk), int(width), int(height),
-                             int(tile_size), tw, th, _p(offs), _p(fl), _p(oc), _p(oa), _p(li))
+                             int(tile_size), tw, th, _p(offs), _p(fl), _p(oc), _p(oa), _p(li),
+                             int(row_step))
     return oc, oa, li
 
 
 def rasterize_to_pixels_bwd(means2d, conics, colors, opacities, betas, width, height,
                             tile_size, isect_offsets, flatten_ids, render_alphas, last_ids,
-                            v_colors, v_alphas, backgrounds=None, masks=None, dtype=np.float32):
+                            v_colors, v_alphas, backgrounds=None, masks=None, dtype=np.float32,
+                            row_step=1):
     means2d, conics, colors = _c(means2d, dtype), _c(conics, dtype), _c(colors, dtype)
     opacities, betas = _c(opacities, dtype), _c(betas, dtype)
     offs = _c(isect_offsets, np.int32)
@@ -255,5 +258,5 @@ def rasterize_to_pixels_bwd(means2d, conics, colors, opacities, betas, width, he
     _fn("raster_bwd", dtype)(C, N, cd, len(fl), _p(means2d), _p(conics), _p(colors),
                              _p(opacities), _p(betas), _p(bg), _p(mk), int(width), int(height),
                              int(tile_size), tw, th, _p(offs), _p(fl), _p(ra), _p(li), _p(vc),
-                             _p(va), _p(vm2), _p(vcn), _p(vcol), _p(vo), _p(vb))
+                             _p(va), _p(vm2), _p(vcn), _p(vcol), _p(vo), _p(vb), int(row_step))
     return vm2, vcn, vcol, vo, vb

@@ -289,3 +289,112 @@ class RefKernels:
             self.launch("rot_bwd", (math.ceil(N / 256),), (256,), 0, [_I64(N), self.p(v_R),
                                                                       self.p(vl)])
         return vl
+
+
+# ------------------------------------------------------------------------
+# The reference's plain render path on its own kernels: autograd Functions
+# with the structure of submodules/gsplat/cuda/_wrapper.py:573-1050 and the
+# call sequence of scene/beta_model.py:660-722 + rendering.py:17-232.
+class RefPipeline:
+    def __init__(self, kernels=None):
+        self.k = kernels or RefKernels()
+        k = self.k
+
+        class Rot(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, l3):
+                return k.rotmat_fwd(l3.contiguous())
+
+            @staticmethod
+            def backward(ctx, vR):
+                return k.rotmat_bwd(vR.contiguous())
+
+        class Covar(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, R, s, l, ri, rj):
+                ctx.save_for_backward(R, s, l, ri, rj)
+                return k.covar_fwd(R.contiguous(), s.contiguous(), l.contiguous(), ri, rj)
+
+            @staticmethod
+            def backward(ctx, v):
+                R, s, l, ri, rj = ctx.saved_tensors
+                vr, vs, vl = k.covar_bwd(R, s, l, ri, rj, v.contiguous())
+                return vr, vs, vl, None, None
+
+        class Cond(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, m, V, o, b, q):
+                args = [t.contiguous() for t in (m, V, o, b, q)]
+                ctx.save_for_backward(*args)
+                return k.cond_fwd(*args)
+
+            @staticmethod
+            def backward(ctx, vm, vV, vo):
+                gm, gV, go, gb = k.cond_bwd(*ctx.saved_tensors, vm.contiguous(), vV.contiguous(),
+                                            vo.contiguous())
+                return gm, gV, go, gb, None
+
+        class Proj(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, means, c6, vms, Ks, W, H):
+                means, c6 = means.contiguous(), c6.contiguous()
+                radii, m2, d, cn, _ = k.projection_fwd(means, c6, vms, Ks, W, H)
+                ctx.save_for_backward(means, c6, vms, Ks, radii, cn)
+                ctx.W, ctx.H = W, H
+                ctx.mark_non_differentiable(radii)
+                return radii, m2, d, cn
+
+            @staticmethod
+            def backward(ctx, vr, vm2, vd, vcn):
+                means, c6, vms, Ks, radii, cn = ctx.saved_tensors
+                C, N = radii.shape
+
+                def z(t, *shape):
+                    return torch.zeros(*shape, device=cn.device) if t is None else t.contiguous()
+                vmeans, vcov, _ = k.projection_bwd(means, c6, vms, Ks, ctx.W, ctx.H, 0.3, radii, cn,
+                                                   z(vm2, C, N, 2), z(vd, C, N), z(vcn, C, N, 3))
+                return vmeans, vcov, None, None, None, None
+
+        class Raster(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, m2, cn, col, op, be, bg, W, H, ts, offs, fl):
+                args = [t.contiguous() for t in (m2, cn, col, op, be)]
+                oc, oa, li = k.raster_fwd(*args, bg, W, H, ts, offs, fl)
+                ctx.save_for_backward(*args, bg, offs, fl, oa, li)
+                ctx.W, ctx.H, ctx.ts = W, H, ts
+                return oc, oa
+
+            @staticmethod
+            def backward(ctx, vc, va):
+                m2, cn, col, op, be, bg, offs, fl, oa, li = ctx.saved_tensors
+                g = k.raster_bwd(m2, cn, col, op, be, bg, ctx.W, ctx.H, ctx.ts, offs, fl, oa, li,
+                                 vc.contiguous(), va.contiguous())
+                return g + (None,) * 6
+
+        self.Rot, self.Covar, self.Cond, self.Proj, self.Raster = Rot, Covar, Cond, Proj, Raster
+
+    def render_view(self, p, viewmat, K, W, H, center, background, rest_i, rest_j, tile_size=16):
+        """Same operator sequence as the reference model's render + rasterization()."""
+        import torch.nn.functional as F
+        scale = F.softplus(p["scale"])
+        beta = 4.0 * torch.exp(p["beta"])
+        view_dir = p["xyz"] - center.unsqueeze(0)
+        query = view_dir / view_dir.norm(dim=-1, keepdim=True)
+        R = self.Rot.apply(p["l_triangle"][:, :3])
+        covar = self.Covar.apply(R, scale, p["l_triangle"], rest_i, rest_j)
+        means_nd = torch.cat([p["xyz"], p["mean"]], -1)
+        opac = torch.sigmoid(p["opacity"])
+        means, convs, opacities = self.Cond.apply(means_nd, covar, opac, beta[:, 1:], query)
+        c6 = convs[..., [0, 0, 0, 1, 1, 2], [0, 1, 2, 1, 2, 2]]
+        vms, Ks = viewmat.unsqueeze(0), K.unsqueeze(0)
+        radii, m2, d, cn = self.Proj.apply(means, c6, vms, Ks, W, H)
+        op = opacities.squeeze(-1).repeat(1, 1)
+        be = beta[:, 0].repeat(1, 1)
+        tw, th = math.ceil(W / tile_size), math.ceil(H / tile_size)
+        with torch.no_grad():
+            _, ids, fl = self.k.isect_tiles(m2.detach(), radii, d.detach(), tile_size, tw, th)
+            offs = self.k.offset_encode(ids, 1, tw, th)
+        colors = p["rgb"].expand(1, -1, -1)
+        oc, oa = self.Raster.apply(m2, cn, colors, op, be, background.unsqueeze(0), W, H,
+                                   tile_size, offs, fl)
+        return oc.permute(0, 3, 1, 2)[0], oa, dict(radii=radii, isect_ids=ids, flatten_ids=fl)

@@ -863,7 +863,8 @@ void offset_encode(int64_t n_isects, const int64_t *isect_ids, int C, uint32_t t
 }
 
 // ------------------------------------------------------- a9: blend forward
-// Per tile, per pixel, front to back over the tile's sorted range:
+// Per tile, per pixel, front to back over the tile's sorted range
+// (row_step > 1 blends only every row_step-th tile row: a timing sample):
 // rasterize_to_pixels_fwd.cu:17-191.  Beta kernel alpha = min(0.999,
 // o * (1 - sigma)^beta) for 0 <= sigma < 1, exclusive termination at T <= 1e-4.
 template <typename T>
@@ -871,7 +872,7 @@ void raster_fwd(int C, int64_t N, int cdim, int64_t n_isects, const T *means2d,
                 const T *conics, const T *colors, const T *opac, const T *betas,
                 const T *bg, const uint8_t *masks, int W, int H, int tile_size,
                 int tw, int th, const int32_t *offsets, const int32_t *flatten_ids,
-                T *out_c, T *out_a, int32_t *last_ids) {
+                T *out_c, T *out_a, int32_t *last_ids, int row_step) {
     const int64_t n_tiles = (int64_t)tw * th;
     (void)N;
 #pragma omp parallel for schedule(dynamic, 4)
@@ -879,6 +880,7 @@ void raster_fwd(int C, int64_t N, int cdim, int64_t n_isects, const T *means2d,
         const int c = (int)(bt / n_tiles);
         const int64_t tile = bt % n_tiles;
         const int ty = (int)(tile / tw), tx = (int)(tile % tw);
+        if (ty % row_step) continue;
         const int32_t rs = offsets[bt];
         const int32_t re = (c == C - 1 && tile == n_tiles - 1) ? (int32_t)n_isects : offsets[bt + 1];
         std::vector<T> acc(cdim);
@@ -930,7 +932,7 @@ void raster_bwd(int C, int64_t N, int cdim, int64_t n_isects, const T *means2d,
                 int tw, int th, const int32_t *offsets, const int32_t *flatten_ids,
                 const T *render_alphas, const int32_t *last_ids, const T *v_colors_out,
                 const T *v_alphas_out, T *v_means2d, T *v_conics, T *v_colors,
-                T *v_opac, T *v_betas) {
+                T *v_opac, T *v_betas, int row_step) {
     const int64_t n_tiles = (int64_t)tw * th;
     (void)N;
     if (n_isects == 0) return;
@@ -940,6 +942,7 @@ void raster_bwd(int C, int64_t N, int cdim, int64_t n_isects, const T *means2d,
         const int c = (int)(bt / n_tiles);
         const int64_t tile = bt % n_tiles;
         const int ty = (int)(tile / tw), tx = (int)(tile % tw);
+        if (ty % row_step) continue;
         const int32_t rs = offsets[bt];
         const int32_t re = (c == C - 1 && tile == n_tiles - 1) ? (int32_t)n_isects : offsets[bt + 1];
         std::vector<T> buf(cdim), vrc(cdim);
@@ -1068,18 +1071,18 @@ void ubso_set_threads(int n) {
                              const T *col, const T *o, const T *b, const T *bg,               \
                              const uint8_t *mk, int W, int H, int ts, int tw, int th,         \
                              const int32_t *off, const int32_t *fl, T *oc, T *oa,             \
-                             int32_t *li) {                                                    \
+                             int32_t *li, int rs) {                                            \
         raster_fwd(C, N, cd, ni, m2, cn, col, o, b, bg, mk, W, H, ts, tw, th, off, fl, oc, oa, \
-                   li);                                                                        \
+                   li, rs < 1 ? 1 : rs);                                                       \
     }                                                                                          \
     void ubso_raster_bwd_##S(int C, int64_t N, int cd, int64_t ni, const T *m2, const T *cn,  \
                              const T *col, const T *o, const T *b, const T *bg,               \
                              const uint8_t *mk, int W, int H, int ts, int tw, int th,         \
                              const int32_t *off, const int32_t *fl, const T *ra,              \
                              const int32_t *li, const T *vc, const T *va, T *vm2, T *vcn,     \
-                             T *vcol, T *vo, T *vb) {                                          \
+                             T *vcol, T *vo, T *vb, int rs) {                                  \
         raster_bwd(C, N, cd, ni, m2, cn, col, o, b, bg, mk, W, H, ts, tw, th, off, fl, ra, li, \
-                   vc, va, vm2, vcn, vcol, vo, vb);                                            \
+                   vc, va, vm2, vcn, vcol, vo, vb, rs < 1 ? 1 : rs);                           \
     }
 
 UBS_ORACLE_BOTH(DEF)

@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol():
     assert not missing, missing
     unbound = [n for n in declared_functions() if n not in _lib.SIGNATURES]
     assert not unbound, "no ctypes signature for %s" % unbound
-    assert lib.ubs_abi_version() == 1
+    assert lib.ubs_abi_version() == 2
 
 
 def test_workspace_queries_and_argument_checks():

@@ -244,8 +244,11 @@ static int device_exclusive_scan(const int32_t *in, OutT *out, int64_t n, int64_
     }
     const int64_t nblocks = (n + SCAN_TILE - 1) / SCAN_TILE;
     scan_blocks_kernel<OutT><<<(unsigned)nblocks, SCAN_THREADS, 0, st>>>(in, out, n, sums);
+    ::ubs::note_launch();
     scan_sums_kernel<<<1, SCAN_THREADS, 0, st>>>(sums, nblocks, total);
+    ::ubs::note_launch();
     if (nblocks > 1) scan_add_kernel<OutT><<<grid_for(n, 256), 256, 0, st>>>(out, n, sums);
+    ::ubs::note_launch();
     return check_launch("exclusive scan");
 }
 
@@ -482,6 +485,7 @@ int ubs_isect_count(int32_t C, int64_t N, const float *means2d, const int32_t *r
             CN, N, reinterpret_cast<const float2 *>(means2d), radii, depths, (float)tile_size,
             (uint32_t)tile_width, (uint32_t)tile_height, tiles_per_gauss, w.bucket_counts,
             &w.hdr->status);
+    ::ubs::note_launch();
     if (int e = check_launch("isect_count")) return e;
     if (int e = device_exclusive_scan<int32_t>(w.bucket_counts, isect_offsets, nb, w.block_sums,
                                                &w.hdr->total, st))
@@ -530,6 +534,7 @@ int ubs_isect_emit(int32_t C, int64_t N, const float *means2d, const int32_t *ra
         isect_emit_ordered_kernel<<<grid_for(CN, 256), 256, 0, st>>>(
             CN, N, m2, radii, depths, ts, (uint32_t)tile_width, (uint32_t)tile_height, tile_bits,
             w.prim_start, isect_ids, flatten_ids, n_isects, &w.cw.hdr->status);
+    ::ubs::note_launch();
         return check_launch("isect_emit_ordered");
     }
     if (cudaMemcpyAsync(w.cursor, isect_offsets, nb * 4, cudaMemcpyDeviceToDevice, st) !=
@@ -539,9 +544,11 @@ int ubs_isect_emit(int32_t C, int64_t N, const float *means2d, const int32_t *ra
     isect_emit_bucket_kernel<<<grid_for(CN, 256), 256, 0, st>>>(
         CN, N, m2, radii, depths, ts, (uint32_t)tile_width, (uint32_t)tile_height, w.cursor,
         w.keys, n_isects, &w.cw.hdr->status);
+    ::ubs::note_launch();
     bucket_sort_small_kernel<<<(unsigned)nb, SORT_THREADS, 0, st>>>(
         nb, (int32_t)n_tiles, tile_bits, isect_offsets, n_isects, w.keys, isect_ids, flatten_ids,
         w.big_list, w.cw.hdr);
+    ::ubs::note_launch();
     if (int e = check_launch("isect bucket sort")) return e;
     // long buckets (their number is only known on the device): a fixed grid
     // walks the device-side list, so the host never waits here
@@ -551,6 +558,7 @@ int ubs_isect_emit(int32_t C, int64_t N, const float *means2d, const int32_t *ra
         bucket_sort_big_kernel<<<grid, BIG_THREADS, 0, st>>>(
             (int32_t)n_tiles, nb, tile_bits, isect_offsets, n_isects, w.keys, w.scratch,
             isect_ids, flatten_ids, w.big_list, w.cw.hdr);
+    ::ubs::note_launch();
     }
     return check_launch("isect big-bucket sort");
 }
@@ -570,6 +578,7 @@ int ubs_isect_offset_encode(int64_t n_isects, const int64_t *isect_ids, int32_t 
     }
     offset_encode_kernel<<<grid_for(nb, 256), 256, 0, st>>>(
         n_isects, isect_ids, nb, (int32_t)n_tiles, bit_width_u32((uint32_t)n_tiles), offsets);
+    ::ubs::note_launch();
     return check_launch("offset_encode");
 }
 

@@ -428,6 +428,7 @@ int ubs_l_triangle_to_rotmat_fwd(int64_t n, const float *l_triangle, int64_t row
     if (n == 0) return UBS_OK;
     rotmat_fwd_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(n, l_triangle,
                                                                           row_stride, rotmats);
+    ::ubs::note_launch();
     return finish("rotmat_fwd");
 }
 
@@ -437,6 +438,7 @@ int ubs_l_triangle_to_rotmat_bwd(int64_t n, const float *v_rotmats, float *v_l_t
     if (n == 0) return UBS_OK;
     rotmat_bwd_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(n, v_rotmats,
                                                                           v_l_triangle);
+    ::ubs::note_launch();
     return finish("rotmat_bwd");
 }
 
@@ -467,6 +469,7 @@ int ubs_rot_scale_l_triangle_to_covar_fwd(int64_t n, int32_t dim, const float *r
     UBS_DIM_SWITCH(dim, covar_fwd_kernel<DD><<<grid_for(n, 128), 128, 0, st>>>(
                             n, rot, scale, l_triangle, rest_i, rest_j, m_rest, spatial_block,
                             covar));
+    ::ubs::note_launch();
     return finish("covar_fwd");
 }
 
@@ -482,6 +485,7 @@ int ubs_rot_scale_l_triangle_to_covar_bwd(int64_t n, int32_t dim, const float *r
     UBS_DIM_SWITCH(dim, covar_bwd_kernel<DD><<<grid_for(n, 128), 128, 0, st>>>(
                             n, rot, scale, l_triangle, rest_i, rest_j, m_rest, spatial_block,
                             v_covar, v_rot, v_scale, v_l_triangle));
+    ::ubs::note_launch();
     return finish("covar_bwd");
 }
 
@@ -507,6 +511,7 @@ int ubs_cond_fwd(int64_t n, int32_t dim, const float *means, const float *covars
     UBS_K_SWITCH(dim - 3, cond_fwd_kernel<KK><<<grid_for(n, 128), 128, 0, st>>>(
                               n, means, covars, opacities, betas, query, out_means, out_covars,
                               out_opacities));
+    ::ubs::note_launch();
     return finish("cond_fwd");
 }
 
@@ -522,6 +527,7 @@ int ubs_cond_bwd(int64_t n, int32_t dim, const float *means, const float *covars
                               n, means, covars, opacities, betas, query, v_out_means,
                               v_out_covars, v_out_opacities, v_means, v_covars, v_opacities,
                               v_betas, exact));
+    ::ubs::note_launch();
     return finish("cond_bwd");
 }
 
@@ -568,6 +574,7 @@ int ubs_projection_fwd(int32_t C, int64_t N, const float *means, const float *co
     const int64_t CN = (int64_t)C * N;
     if (CN == 0) return UBS_OK;
     projection_fwd_kernel<<<grid_for(CN, 256), 256, 0, (cudaStream_t)stream>>>(a);
+    ::ubs::note_launch();
     return finish("projection_fwd");
 }
 
@@ -612,6 +619,7 @@ int ubs_projection_bwd(int32_t C, int64_t N, const float *means, const float *co
     const int64_t CN = (int64_t)C * N;
     if (CN == 0) return UBS_OK;
     projection_bwd_kernel<<<grid_for(CN, 256), 256, 0, st>>>(a);
+    ::ubs::note_launch();
     return finish("projection_bwd");
 }
 

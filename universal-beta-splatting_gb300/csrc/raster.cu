@@ -51,6 +51,7 @@ struct RasterArgs {
     const float *v_out_a;
     float *v_m2, *v_cn, *v_col, *v_op, *v_be;
     uint32_t *status;
+    unsigned long long *pair_count; // contributing (pixel, record) pairs, or nullptr
 };
 
 // ---------------------------------------------------------------- packing
@@ -202,6 +203,7 @@ __global__ void __launch_bounds__(1024) raster_fwd_kernel(RasterArgs a) {
     const float px = (float)j + 0.5f, py = (float)i + 0.5f;
     float T = 1.0f;
     int32_t cur = 0;
+    uint32_t n_contrib = 0;
     float acc[CD];
 #pragma unroll
     for (int k = 0; k < CD; ++k) acc[k] = 0.f;
@@ -278,6 +280,7 @@ __global__ void __launch_bounds__(1024) raster_fwd_kernel(RasterArgs a) {
                                     }
                                     cur = bs + t;
                                     T = next_T;
+                                    ++n_contrib;
                                 }
                             }
                         }
@@ -297,6 +300,10 @@ __global__ void __launch_bounds__(1024) raster_fwd_kernel(RasterArgs a) {
                     atomicOr(a.status, DEV_ERR_WAIT_TIMEOUT);
     }
 
+    if (a.pair_count) {
+        const uint32_t w = __reduce_add_sync(0xffffffffu, n_contrib);
+        if (lane == 0 && w) atomicAdd(a.pair_count, (unsigned long long)w);
+    }
     if (inside) {
         a.out_a[pix] = 1.0f - T;
 #pragma unroll
@@ -529,27 +536,23 @@ size_t raster_ws_bytes(int64_t T, int ch) {
     return b;
 }
 
-struct RasterHost {
-    RasterArgs a;
-    int channels;
-    cudaStream_t st;
-};
+template <int CD>
+static int launch_pack(int64_t T, int64_t n_prims, const int32_t *fl, const float *m2,
+                       const float *cn, const float *op, const float *be, const float *col,
+                       GeoRec *recs, float4 *rcols, uint32_t *status, cudaStream_t st) {
+    constexpr bool PACK = CD <= 4;
+    const int blk = 256;
+    const int64_t nblk = (T + blk - 1) / blk;
+    const unsigned grid = (unsigned)(nblk < 152 * 16 ? nblk : 152 * 16);
+    pack_records_kernel<CD, PACK><<<grid, blk, 0, st>>>(T, n_prims, fl, m2, cn, op, be, col,
+                                                       recs, PACK ? rcols : nullptr, status);
+    note_launch();
+    return check_launch("pack_records");
+}
 
 template <int CD, bool BWD>
-static int launch_raster(RasterArgs &a, int64_t T, const int32_t *fl, const float *m2,
-                         const float *cn, const float *op, const float *be, const float *col,
-                         cudaStream_t st) {
+static int launch_blend(RasterArgs &a, cudaStream_t st) {
     constexpr bool PACK = CD <= 4;
-    // pack sorted records
-    if (T > 0) {
-        const int blk = 256;
-        const int64_t nblk = (T + blk - 1) / blk;
-        const unsigned grid = (unsigned)(nblk < 152 * 16 ? nblk : 152 * 16);
-        pack_records_kernel<CD, PACK><<<grid, blk, 0, st>>>(
-            T, a.n_prims, fl, m2, cn, op, be, col, const_cast<GeoRec *>(a.recs),
-            const_cast<float4 *>(a.rcols), a.status);
-        if (int e = check_launch("pack_records")) return e;
-    }
     const int B = a.TS * a.TS;
     const SmemLayout L = smem_layout<CD, PACK, BWD>(B);
     if (L.total > 227 * 1024)
@@ -557,51 +560,44 @@ static int launch_raster(RasterArgs &a, int64_t T, const int32_t *fl, const floa
                                               "of shared memory", a.TS, CD, L.total);
     const unsigned nblocks = (unsigned)((int64_t)a.C * a.n_tiles);
     if (nblocks == 0) return UBS_OK;
-    if (BWD) {
-        auto k = raster_bwd_kernel<CD, PACK>;
-        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total) !=
-            cudaSuccess)
-            return check_launch("raster_bwd smem attribute");
-        k<<<nblocks, B, L.total, st>>>(a);
-        return check_launch("raster_bwd");
-    } else {
-        auto k = raster_fwd_kernel<CD, PACK>;
-        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total) !=
-            cudaSuccess)
-            return check_launch("raster_fwd smem attribute");
-        k<<<nblocks, B, L.total, st>>>(a);
-        return check_launch("raster_fwd");
-    }
+    auto k = BWD ? raster_bwd_kernel<CD, PACK> : raster_fwd_kernel<CD, PACK>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total) !=
+        cudaSuccess)
+        return check_launch("raster smem attribute");
+    k<<<nblocks, B, L.total, st>>>(a);
+    note_launch();
+    return check_launch(BWD ? "raster_bwd" : "raster_fwd");
 }
 
-template <bool BWD>
-static int dispatch_raster(int ch, RasterArgs &a, int64_t T, const int32_t *fl,
-                           const float *m2, const float *cn, const float *op, const float *be,
-                           const float *col, cudaStream_t st) {
-#define UBS_CASE(n)                                                                       \
-    case n:                                                                               \
-        return launch_raster<n, BWD>(a, T, fl, m2, cn, op, be, col, st);
+#define UBS_CHANNEL_SWITCH(ch, ...)                                                        \
+    switch (ch) {                                                                          \
+    case 1: { constexpr int CDV = 1; __VA_ARGS__; }                                        \
+    case 2: { constexpr int CDV = 2; __VA_ARGS__; }                                        \
+    case 3: { constexpr int CDV = 3; __VA_ARGS__; }                                        \
+    case 4: { constexpr int CDV = 4; __VA_ARGS__; }                                        \
+    case 5: { constexpr int CDV = 5; __VA_ARGS__; }                                        \
+    case 8: { constexpr int CDV = 8; __VA_ARGS__; }                                        \
+    case 9: { constexpr int CDV = 9; __VA_ARGS__; }                                        \
+    case 16: { constexpr int CDV = 16; __VA_ARGS__; }                                      \
+    case 17: { constexpr int CDV = 17; __VA_ARGS__; }                                      \
+    case 32: { constexpr int CDV = 32; __VA_ARGS__; }                                      \
+    case 33: { constexpr int CDV = 33; __VA_ARGS__; }                                      \
+    default: return set_error(UBS_ERR_UNSUPPORTED, "raster: %d channels", ch);           \
+    }
+
+static bool channels_ok(int ch) {
     switch (ch) {
-        UBS_CASE(1) UBS_CASE(2) UBS_CASE(3) UBS_CASE(4) UBS_CASE(5) UBS_CASE(8) UBS_CASE(9)
-        UBS_CASE(16) UBS_CASE(17) UBS_CASE(32) UBS_CASE(33)
+    case 1: case 2: case 3: case 4: case 5: case 8: case 9:
+    case 16: case 17: case 32: case 33:
+        return true;
     default:
-        return set_error(UBS_ERR_UNSUPPORTED, "raster: %d channels", ch);
+        return false;
     }
-#undef UBS_CASE
 }
 
-static int validate_raster(int32_t C, int64_t N, int32_t ch, int64_t T, int32_t W, int32_t H,
-                           int32_t ts, int32_t tw, int32_t th, void *ws, size_t ws_bytes) {
-    UBS_REQUIRE(C >= 1 && N >= 0 && W >= 0 && H >= 0, "raster: bad sizes C=%d N=%lld W=%d H=%d",
-                C, (long long)N, W, H);
+static int validate_ws(int32_t ch, int64_t T, void *ws, size_t ws_bytes) {
     UBS_REQUIRE(T >= 0 && T < (1ll << 31), "raster: n_isects %lld out of range", (long long)T);
-    UBS_REQUIRE((int64_t)C * N < (1ll << 31), "raster: C*N must fit in int32");
-    if (!(ts == 8 || ts == 16 || ts == 24 || ts == 32))
-        return set_error(UBS_ERR_UNSUPPORTED, "raster: tile_size %d (supported 8, 16, 24, 32)",
-                         ts);
-    UBS_REQUIRE((int64_t)tw * ts >= W && (int64_t)th * ts >= H,
-                "raster: tile grid %dx%d of %d px does not cover %dx%d", tw, th, ts, W, H);
-    if (!channels_supported(ch))
+    if (!channels_ok(ch))
         return set_error(UBS_ERR_UNSUPPORTED, "raster: %d channels (supported 1-5, 8, 9, 16, "
                                               "17, 32, 33)", ch);
     UBS_REQUIRE(ws != nullptr && ((uintptr_t)ws & 255) == 0,
@@ -610,6 +606,19 @@ static int validate_raster(int32_t C, int64_t N, int32_t ch, int64_t T, int32_t 
         return set_error(UBS_ERR_OVERFLOW, "raster: workspace %zu B < %zu B needed", ws_bytes,
                          raster_ws_bytes(T, ch));
     return UBS_OK;
+}
+
+static int validate_raster(int32_t C, int64_t N, int32_t ch, int64_t T, int32_t W, int32_t H,
+                           int32_t ts, int32_t tw, int32_t th, void *ws, size_t ws_bytes) {
+    UBS_REQUIRE(C >= 1 && N >= 0 && W >= 0 && H >= 0, "raster: bad sizes C=%d N=%lld W=%d H=%d",
+                C, (long long)N, W, H);
+    UBS_REQUIRE((int64_t)C * N < (1ll << 31), "raster: C*N must fit in int32");
+    if (!(ts == 8 || ts == 16 || ts == 24 || ts == 32))
+        return set_error(UBS_ERR_UNSUPPORTED, "raster: tile_size %d (supported 8, 16, 24, 32)",
+                         ts);
+    UBS_REQUIRE(tw >= 1 && th >= 1 && (int64_t)tw * ts >= W && (int64_t)th * ts >= H,
+                "raster: tile grid %dx%d of %d px does not cover %dx%d", tw, th, ts, W, H);
+    return validate_ws(ch, T, ws, ws_bytes);
 }
 
 static void fill_common(RasterArgs &a, int32_t C, int64_t N, int32_t ch, int64_t T, int32_t W,
@@ -632,6 +641,7 @@ static void fill_common(RasterArgs &a, int32_t C, int64_t N, int32_t ch, int64_t
     a.colors = colors;
     a.bg = bg;
     a.masks = masks;
+    a.pair_count = nullptr;
 }
 
 } // namespace ubs
@@ -644,6 +654,82 @@ size_t ubs_raster_workspace_bytes(int64_t n_isects, int32_t channels) {
     return raster_ws_bytes(n_isects < 0 ? 0 : n_isects, channels);
 }
 
+int ubs_raster_pack(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
+                    const int32_t *flatten_ids, const float *means2d, const float *conics,
+                    const float *opacities, const float *betas, const float *colors,
+                    void *workspace, size_t workspace_bytes, void *stream) {
+    UBS_REQUIRE(C >= 1 && N >= 0 && (int64_t)C * N < (1ll << 31), "raster_pack: bad sizes");
+    if (int e = validate_ws(channels, n_isects, workspace, workspace_bytes)) return e;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    unsigned char *w = static_cast<unsigned char *>(workspace);
+    if (cudaMemsetAsync(w, 0, 256, st) != cudaSuccess) return check_launch("raster_pack memset");
+    if (n_isects == 0) return UBS_OK;
+    GeoRec *recs = reinterpret_cast<GeoRec *>(w + 256);
+    float4 *rcols = reinterpret_cast<float4 *>(w + 256 + n_isects * sizeof(GeoRec));
+    uint32_t *status = reinterpret_cast<uint32_t *>(w);
+    const int64_t P = (int64_t)C * N;
+    UBS_CHANNEL_SWITCH(channels, return launch_pack<CDV>(n_isects, P, flatten_ids, means2d,
+                                                         conics, opacities, betas, colors, recs,
+                                                         rcols, status, st));
+}
+
+int ubs_raster_fwd_packed(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
+                          const float *colors, const float *backgrounds, const uint8_t *masks,
+                          int32_t width, int32_t height, int32_t tile_size, int32_t tile_width,
+                          int32_t tile_height, const int32_t *isect_offsets,
+                          float *render_colors, float *render_alphas, int32_t *last_ids,
+                          int32_t count_pairs, void *workspace, size_t workspace_bytes,
+                          void *stream) {
+    if (int e = validate_raster(C, N, channels, n_isects, width, height, tile_size, tile_width,
+                                tile_height, workspace, workspace_bytes))
+        return e;
+    RasterArgs a{};
+    fill_common(a, C, N, channels, n_isects, width, height, tile_size, tile_width, tile_height,
+                isect_offsets, colors, backgrounds, masks, workspace);
+    a.out_c = render_colors;
+    a.out_a = render_alphas;
+    a.last_ids = last_ids;
+    if (count_pairs)
+        a.pair_count = reinterpret_cast<unsigned long long *>(static_cast<unsigned char *>(workspace) + 8);
+    UBS_CHANNEL_SWITCH(channels, return launch_blend<CDV, false>(a, static_cast<cudaStream_t>(stream)));
+}
+
+int ubs_raster_bwd_packed(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
+                          const float *colors, const float *backgrounds, const uint8_t *masks,
+                          int32_t width, int32_t height, int32_t tile_size, int32_t tile_width,
+                          int32_t tile_height, const int32_t *isect_offsets,
+                          const float *render_alphas, const int32_t *last_ids,
+                          const float *v_render_colors, const float *v_render_alphas,
+                          float *v_means2d, float *v_conics, float *v_colors, float *v_opacities,
+                          float *v_betas, int32_t zero_outputs, void *workspace,
+                          size_t workspace_bytes, void *stream) {
+    if (int e = validate_raster(C, N, channels, n_isects, width, height, tile_size, tile_width,
+                                tile_height, workspace, workspace_bytes))
+        return e;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int64_t P = (int64_t)C * N;
+    if (zero_outputs &&
+        (cudaMemsetAsync(v_means2d, 0, P * 2 * 4, st) ||
+         cudaMemsetAsync(v_conics, 0, P * 3 * 4, st) ||
+         cudaMemsetAsync(v_colors, 0, P * channels * 4, st) ||
+         cudaMemsetAsync(v_opacities, 0, P * 4, st) || cudaMemsetAsync(v_betas, 0, P * 4, st)))
+        return check_launch("raster_bwd memset");
+    if (n_isects == 0) return UBS_OK;
+    RasterArgs a{};
+    fill_common(a, C, N, channels, n_isects, width, height, tile_size, tile_width, tile_height,
+                isect_offsets, colors, backgrounds, masks, workspace);
+    a.render_alphas = render_alphas;
+    a.last_in = last_ids;
+    a.v_out_c = v_render_colors;
+    a.v_out_a = v_render_alphas;
+    a.v_m2 = v_means2d;
+    a.v_cn = v_conics;
+    a.v_col = v_colors;
+    a.v_op = v_opacities;
+    a.v_be = v_betas;
+    UBS_CHANNEL_SWITCH(channels, return launch_blend<CDV, true>(a, st));
+}
+
 int ubs_raster_fwd(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
                    const float *means2d, const float *conics, const float *colors,
                    const float *opacities, const float *betas, const float *backgrounds,
@@ -654,16 +740,13 @@ int ubs_raster_fwd(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
     if (int e = validate_raster(C, N, channels, n_isects, width, height, tile_size, tile_width,
                                 tile_height, workspace, workspace_bytes))
         return e;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    RasterArgs a{};
-    fill_common(a, C, N, channels, n_isects, width, height, tile_size, tile_width, tile_height,
-                isect_offsets, colors, backgrounds, masks, workspace);
-    a.out_c = render_colors;
-    a.out_a = render_alphas;
-    a.last_ids = last_ids;
-    if (cudaMemsetAsync(a.status, 0, 4, st) != cudaSuccess) return check_launch("memset");
-    return dispatch_raster<false>(channels, a, n_isects, flatten_ids, means2d, conics, opacities,
-                                  betas, colors, st);
+    if (int e = ubs_raster_pack(C, N, channels, n_isects, flatten_ids, means2d, conics,
+                                opacities, betas, colors, workspace, workspace_bytes, stream))
+        return e;
+    return ubs_raster_fwd_packed(C, N, channels, n_isects, colors, backgrounds, masks, width,
+                                 height, tile_size, tile_width, tile_height, isect_offsets,
+                                 render_colors, render_alphas, last_ids, 0, workspace,
+                                 workspace_bytes, stream);
 }
 
 int ubs_raster_bwd(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
@@ -679,37 +762,26 @@ int ubs_raster_bwd(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
     if (int e = validate_raster(C, N, channels, n_isects, width, height, tile_size, tile_width,
                                 tile_height, workspace, workspace_bytes))
         return e;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int64_t P = (int64_t)C * N;
-    if (cudaMemsetAsync(v_means2d, 0, P * 2 * 4, st) ||
-        cudaMemsetAsync(v_conics, 0, P * 3 * 4, st) ||
-        cudaMemsetAsync(v_colors, 0, P * channels * 4, st) ||
-        cudaMemsetAsync(v_opacities, 0, P * 4, st) || cudaMemsetAsync(v_betas, 0, P * 4, st))
-        return check_launch("raster_bwd memset");
-    if (n_isects == 0) return UBS_OK;
-    RasterArgs a{};
-    fill_common(a, C, N, channels, n_isects, width, height, tile_size, tile_width, tile_height,
-                isect_offsets, colors, backgrounds, masks, workspace);
-    a.render_alphas = render_alphas;
-    a.last_in = last_ids;
-    a.v_out_c = v_render_colors;
-    a.v_out_a = v_render_alphas;
-    a.v_m2 = v_means2d;
-    a.v_cn = v_conics;
-    a.v_col = v_colors;
-    a.v_op = v_opacities;
-    a.v_be = v_betas;
-    if (cudaMemsetAsync(a.status, 0, 4, st) != cudaSuccess) return check_launch("memset");
-    return dispatch_raster<true>(channels, a, n_isects, flatten_ids, means2d, conics, opacities,
-                                 betas, colors, st);
+    if (int e = ubs_raster_pack(C, N, channels, n_isects, flatten_ids, means2d, conics,
+                                opacities, betas, colors, workspace, workspace_bytes, stream))
+        return e;
+    return ubs_raster_bwd_packed(C, N, channels, n_isects, colors, backgrounds, masks, width,
+                                 height, tile_size, tile_width, tile_height, isect_offsets,
+                                 render_alphas, last_ids, v_render_colors, v_render_alphas,
+                                 v_means2d, v_conics, v_colors, v_opacities, v_betas, 1,
+                                 workspace, workspace_bytes, stream);
 }
 
-int ubs_raster_status(const void *workspace, uint32_t *status, void *stream) {
+int ubs_raster_status(const void *workspace, uint32_t *status, uint64_t *pair_count,
+                      void *stream) {
     UBS_REQUIRE(workspace && status, "raster_status: null pointer");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (cudaMemcpyAsync(status, workspace, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+    uint64_t hdr[2];
+    if (cudaMemcpyAsync(hdr, workspace, 16, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
         return check_launch("raster_status");
+    *status = (uint32_t)(hdr[0] & 0xffffffffu);
+    if (pair_count) *pair_count = hdr[1];
     return UBS_OK;
 }
 

@@ -12,6 +12,8 @@ namespace ubs {
 // The last error message of the calling host thread (read by ubs_last_error).
 int set_error(int code, const char *fmt, ...);
 int check_launch(const char *what);
+// Counts kernel launches made by this library (read with ubs_launch_count).
+void note_launch(int n = 1);
 
 #define UBS_REQUIRE(cond, ...)                                                  \
     do {                                                                        \

@@ -423,10 +423,15 @@ class _RasterizeToPixels(torch.autograd.Function):
         render_alphas = torch.empty(C, height, width, 1, device=dev)
         last_ids = torch.empty(C, height, width, dtype=torch.int32, device=dev)
         ws = L.workspace(L.query("ubs_raster_workspace_bytes", T, ch), dev)
-        L.call("ubs_raster_fwd", C, N, ch, T, L.ptr(means2d), L.ptr(conics), L.ptr(colors),
-               L.ptr(opacities), L.ptr(betas), L.ptr(backgrounds), L.ptr(mask_u8), width, height,
-               tile_size, tw, th, L.ptr(offsets), L.ptr(flatten_ids), L.ptr(render_colors),
-               L.ptr(render_alphas), L.ptr(last_ids), L.ptr(ws), ws.numel(), L.stream(dev))
+        st = L.stream(dev)
+        # one record per sorted intersection; the backward reuses the same records
+        L.call("ubs_raster_pack", C, N, ch, T, L.ptr(flatten_ids), L.ptr(means2d), L.ptr(conics),
+               L.ptr(opacities), L.ptr(betas), L.ptr(colors), L.ptr(ws), ws.numel(), st)
+        L.call("ubs_raster_fwd_packed", C, N, ch, T, L.ptr(colors), L.ptr(backgrounds),
+               L.ptr(mask_u8), width, height, tile_size, tw, th, L.ptr(offsets),
+               L.ptr(render_colors), L.ptr(render_alphas), L.ptr(last_ids), 0, L.ptr(ws),
+               ws.numel(), st)
+        ctx.ws = ws
         ctx.save_for_backward(means2d, conics, colors, opacities, betas, backgrounds, mask_u8,
                               offsets, flatten_ids, render_alphas, last_ids)
         ctx.width, ctx.height, ctx.tile_size = width, height, tile_size
@@ -447,18 +452,18 @@ class _RasterizeToPixels(torch.autograd.Function):
             v_render_alphas = torch.zeros(C, ctx.height, ctx.width, 1, device=dev)
         v_render_colors = _f32(v_render_colors)
         v_render_alphas = _f32(v_render_alphas)
-        v_means2d = torch.empty_like(means2d)
-        v_conics = torch.empty_like(conics)
-        v_colors = torch.empty_like(colors)
-        v_opacities = torch.empty_like(opacities)
-        v_betas = torch.empty_like(betas)
-        ws = L.workspace(L.query("ubs_raster_workspace_bytes", T, ch), dev)
-        L.call("ubs_raster_bwd", C, N, ch, T, L.ptr(means2d), L.ptr(conics), L.ptr(colors),
-               L.ptr(opacities), L.ptr(betas), L.ptr(backgrounds), L.ptr(mask_u8), ctx.width,
-               ctx.height, ctx.tile_size, tw, th, L.ptr(offsets), L.ptr(flatten_ids),
+        v_means2d = torch.zeros_like(means2d)
+        v_conics = torch.zeros_like(conics)
+        v_colors = torch.zeros_like(colors)
+        v_opacities = torch.zeros_like(opacities)
+        v_betas = torch.zeros_like(betas)
+        ws = ctx.ws
+        L.call("ubs_raster_bwd_packed", C, N, ch, T, L.ptr(colors), L.ptr(backgrounds),
+               L.ptr(mask_u8), ctx.width, ctx.height, ctx.tile_size, tw, th, L.ptr(offsets),
                L.ptr(render_alphas), L.ptr(last_ids), L.ptr(v_render_colors),
                L.ptr(v_render_alphas), L.ptr(v_means2d), L.ptr(v_conics), L.ptr(v_colors),
-               L.ptr(v_opacities), L.ptr(v_betas), L.ptr(ws), ws.numel(), L.stream(dev))
+               L.ptr(v_opacities), L.ptr(v_betas), 0, L.ptr(ws), ws.numel(), L.stream(dev))
+        ctx.ws = None
         v_backgrounds = None
         if ctx.needs_input_grad[5]:
             v_backgrounds = (v_render_colors * (1.0 - render_alphas).float()).sum(dim=(1, 2))

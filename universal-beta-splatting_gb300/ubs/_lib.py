@@ -48,7 +48,15 @@ SIGNATURES = {
                        _INT),
     "ubs_raster_bwd": ([_I32, _I64, _I32, _I64] + [_P] * 7 + [_I32] * 5 + [_P] * 2 + [_P] * 4
                        + [_P] * 5 + [_P, _SZ, _P], _INT),
-    "ubs_raster_status": ([_P, _U32P, _P], _INT),
+    "ubs_raster_pack": ([_I32, _I64, _I32, _I64] + [_P] * 6 + [_P, _SZ, _P], _INT),
+    "ubs_raster_fwd_packed": ([_I32, _I64, _I32, _I64] + [_P] * 3 + [_I32] * 5 + [_P] * 4
+                              + [_I32, _P, _SZ, _P], _INT),
+    "ubs_raster_bwd_packed": ([_I32, _I64, _I32, _I64] + [_P] * 3 + [_I32] * 5 + [_P] * 3
+                              + [_P] * 2 + [_P] * 5 + [_I32, _P, _SZ, _P], _INT),
+    "ubs_raster_status": ([_P, _U32P, ctypes.POINTER(ctypes.c_uint64), _P], _INT),
+    "ubs_launch_count": ([], ctypes.c_ulonglong),
+    "ubs_fp32_probe_workspace_bytes": ([], _SZ),
+    "ubs_fp32_probe": ([_I32, _P, _SZ, ctypes.POINTER(ctypes.c_double), _P], _INT),
 }
 
 _lib = None
