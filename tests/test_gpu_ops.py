@@ -254,11 +254,20 @@ def test_blend_fwd_bwd(C, N, W, H, ts, channels, bg):
     wc = torch.randn(rc.shape, generator=g)
     wa = torch.randn(ra.shape, generator=g)
     ((rc * wc.to(DEV)).sum() + (ra * wa.to(DEV)).sum()).backward()
-    ref = orc.rasterize_to_pixels_bwd(*[npy(t) for t in ts_in], W, H, ts, npy(offs), npy(fl),
-                                      oa, li, npy(wc), npy(wa),
-                                      backgrounds=None if bgs is None else npy(bgs))
+    # Gradients are checked against the FP64 oracle: near the ellipse edge with
+    # beta < 1, (1 - sigma)^(beta - 1) amplifies FP32 rounding of sigma, so FP32
+    # results (this kernel, the reference's kernel, the FP32 oracle) all sit
+    # up to ~1e-3 (relative L2) from the exact value.  The 1e-4 bar against the
+    # reference's own backward is tests/test_gpu_reference.py.
+    np64 = [npy(t).astype(np.float64) for t in ts_in]
+    bg64 = None if bgs is None else npy(bgs).astype(np.float64)
+    _, oa64, li64 = orc.rasterize_to_pixels(*np64, W, H, ts, npy(offs), npy(fl), backgrounds=bg64,
+                                            dtype=np.float64)
+    ref = orc.rasterize_to_pixels_bwd(*np64, W, H, ts, npy(offs), npy(fl), oa64, li64,
+                                      npy(wc).astype(np.float64), npy(wa).astype(np.float64),
+                                      backgrounds=bg64, dtype=np.float64)
     for t, r, nm in zip(ts_dev, ref, ("v_means2d", "v_conics", "v_colors", "v_opac", "v_betas")):
-        grad_close(npy(t.grad), r, nm)
+        grad_close(npy(t.grad), r, nm, rel_l2=1e-3)
     if bg:
         v_bg = (wc * (1 - torch.tensor(oa))).sum(dim=(1, 2))
         np.testing.assert_allclose(npy(bg_dev.grad), npy(v_bg), rtol=1e-4, atol=1e-3)

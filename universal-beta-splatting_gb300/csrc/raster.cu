@@ -10,8 +10,11 @@
 //     front-to-back list as one contiguous span;
 //   * each CTA streams its span through shared memory with bulk async copies
 //     (cp.async.bulk + mbarrier, double-buffered, bounded waits);
+//   * each thread owns two vertically adjacent pixels (a warp an 8x8 block),
+//     so record loads, loop control and the backward's warp reductions are
+//     shared by two pixels;
 //   * every batch, each record's ellipse bounding box is tested against the
-//     8x4-pixel footprint of every warp and turned into per-warp bitmasks by
+//     8x8-pixel footprint of every warp and turned into per-warp bitmasks by
 //     ballot, so a warp only visits records that can touch its pixels;
 //   * the backward sums the 7 + channels gradients of a record over a warp with
 //     a transpose reduction (16 shuffles for 16 values), accumulates warps in
@@ -93,23 +96,27 @@ __global__ void pack_records_kernel(int64_t T, int64_t n_prims, const int32_t *_
 }
 
 // ------------------------------------------------------ shared helpers
+// Thread layout: every thread owns two vertically adjacent pixels, a warp an
+// 8x8-pixel footprint; a TS x TS tile has (TS/8)^2 warps = TS*TS/2 threads and
+// streams its records in batches of TS*TS, two batch slots per thread in the
+// culling phase.
 struct SmemLayout {
     int mask_off, rec_off, col_off, gacc_off, touched_off, total;
 };
 
 template <int CD, bool PACK, bool BWD>
-__host__ __device__ inline SmemLayout smem_layout(int B) {
-    constexpr int NV = 7 + CD;
-    constexpr int NG = (NV + 15) / 16;
-    const int nw = B / 32;
+__host__ __device__ inline SmemLayout smem_layout(int NT) {
+    constexpr int NV = 7 + CD; // gradient values per record
+    const int nw = NT / 32, BR = 2 * NT;
     SmemLayout L;
-    L.mask_off = 16;                                         // after 2 mbarriers
-    L.rec_off = (L.mask_off + nw * nw * 4 + nw * 4 + 127) & ~127;
+    L.mask_off = 16; // after two mbarriers
+    // per-target-warp masks (nw x 2nw words), then one int per warp
+    L.rec_off = (L.mask_off + nw * 2 * nw * 4 + nw * 4 + 127) & ~127;
     const int colbytes = PACK ? 16 : CD * 4;
-    L.col_off = L.rec_off + 2 * B * (int)sizeof(GeoRec);
-    L.gacc_off = (L.col_off + 2 * B * colbytes + 15) & ~15;
-    L.touched_off = L.gacc_off + (BWD ? B * NG * 16 * 4 : 0);
-    L.total = L.touched_off + (BWD ? B * 4 : 0);
+    L.col_off = L.rec_off + 2 * BR * (int)sizeof(GeoRec);
+    L.gacc_off = (L.col_off + 2 * BR * colbytes + 15) & ~15;
+    L.touched_off = L.gacc_off + (BWD ? BR * NV * 4 : 0);
+    L.total = L.touched_off + (BWD ? BR * 4 : 0);
     return L;
 }
 
@@ -129,43 +136,92 @@ __device__ __forceinline__ bool conic_box(const GeoRec &r, float &ex, float &ey)
 // Issues the bulk copies of batch [bs, bs+cnt) into buffer `buf` (thread 0).
 template <bool PACK>
 __device__ __forceinline__ void issue_batch(const RasterArgs &a, GeoRec *srec, float4 *scol4,
-                                            uint64_t *mbar, int B, int buf, int32_t bs,
+                                            uint64_t *mbar, int BR, int buf, int32_t bs,
                                             int cnt) {
     fence_proxy_async_smem();
     const uint32_t bytes = (uint32_t)cnt * (32u + (PACK ? 16u : 0u));
     mbar_arrive_expect_tx(&mbar[buf], bytes);
-    bulk_g2s(srec + buf * B, a.recs + bs, (uint32_t)cnt * 32u, &mbar[buf]);
-    if (PACK) bulk_g2s(scol4 + buf * B, a.rcols + bs, (uint32_t)cnt * 16u, &mbar[buf]);
+    bulk_g2s(srec + buf * BR, a.recs + bs, (uint32_t)cnt * 32u, &mbar[buf]);
+    if (PACK) bulk_g2s(scol4 + buf * BR, a.rcols + bs, (uint32_t)cnt * 16u, &mbar[buf]);
 }
 
-// Per-batch culling masks.  Thread tid describes record tid of the batch;
-// for every warp w of the CTA one ballot gives the 32 bits of this thread's
-// warp in w's mask.  limit[w] bounds the record index for warp w (backward).
-__device__ __forceinline__ void build_masks(const GeoRec &r, bool valid, int idx, int nw,
-                                            int wpr, int tile_x0, int tile_y0, int warp,
-                                            int lane, uint32_t *wmask, const int32_t *limit) {
-    float ex = 0.f, ey = 0.f;
-    const bool boxed = valid && conic_box(r, ex, ey);
-    for (int w = 0; w < nw; ++w) {
-        const float x0 = (float)(tile_x0 + (w % wpr) * 8) + 0.5f;
-        const float y0 = (float)(tile_y0 + (w / wpr) * 4) + 0.5f;
-        bool ov = valid;
-        if (boxed)
-            ov = (r.x - ex <= x0 + 7.f) && (r.x + ex >= x0) && (r.y - ey <= y0 + 3.f) &&
-                 (r.y + ey >= y0);
-        if (limit) ov = ov && (idx <= limit[w]);
-        const uint32_t word = __ballot_sync(0xffffffffu, ov);
-        if (lane == 0) wmask[w * nw + warp] = word;
+// Per-batch culling masks.  Thread tid describes batch slots tid and tid + NT;
+// for every warp w one ballot per slot gives 32 bits of w's 2*nw-word mask
+// (word k covers slots 32k .. 32k+31, so ascending bits are front to back).
+// limit[w] (backward) drops records past warp w's last contributor.
+__device__ __forceinline__ void build_masks(const GeoRec *batch, int cnt, int lo, int NT, int nw,
+                                            int wpr, int tile_x0, int tile_y0, int tid, int lane,
+                                            uint32_t *wmask, const int32_t *limit) {
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        const int s = tid + half * NT;
+        const bool valid = s < cnt;
+        GeoRec r;
+        float ex = 0.f, ey = 0.f;
+        bool boxed = false;
+        if (valid) {
+            r = batch[s];
+            boxed = conic_box(r, ex, ey);
+        }
+        const int word = s >> 5;
+        for (int w = 0; w < nw; ++w) {
+            const float x0 = (float)(tile_x0 + (w % wpr) * 8) + 0.5f;
+            const float y0 = (float)(tile_y0 + (w / wpr) * 8) + 0.5f;
+            bool ov = valid;
+            if (boxed)
+                ov = (r.x - ex <= x0 + 7.f) && (r.x + ex >= x0) && (r.y - ey <= y0 + 7.f) &&
+                     (r.y + ey >= y0);
+            if (limit) ov = ov && (lo + s <= limit[w]);
+            const uint32_t bits = __ballot_sync(0xffffffffu, ov);
+            if (lane == 0) wmask[w * 2 * nw + word] = bits;
+        }
     }
+}
+
+template <int CD, bool PACK>
+__device__ __forceinline__ void load_color(const float4 *scol4, const float *scol, int slot,
+                                           float (&col)[CD]) {
+    if (PACK) {
+        const float4 c = scol4[slot];
+        col[0] = c.x;
+        if (CD > 1) col[1 % CD] = c.y;
+        if (CD > 2) col[2 % CD] = c.z;
+        if (CD > 3) col[3 % CD] = c.w;
+    } else {
+#pragma unroll
+        for (int k = 0; k < CD; ++k) col[k] = scol[slot * CD + k];
+    }
+}
+
+// One front-to-back blend step of one pixel (rasterize_to_pixels_fwd.cu:139-171).
+template <int CD>
+__device__ __forceinline__ void blend_one(const GeoRec &q, const float (&col)[CD], float px,
+                                          float py, float &T, float (&acc)[CD], int32_t &cur,
+                                          bool &done, int32_t idx, uint32_t &n_contrib) {
+    if (done) return;
+    const float dx = q.x - px, dy = q.y - py;
+    const float sigma = (q.cxx * dx * dx + q.cyy * dy * dy) + 2.f * q.cxy * dx * dy;
+    if (sigma < 0.f || sigma >= 1.f) return;
+    const float alpha = fminf(0.999f, q.opac * __powf(1.f - sigma, q.beta));
+    const float next_T = T * (1.f - alpha);
+    if (next_T <= 1e-4f) {
+        done = true;
+        return;
+    }
+    const float vis = alpha * T;
+#pragma unroll
+    for (int k = 0; k < CD; ++k) acc[k] += col[k] * vis;
+    cur = idx;
+    T = next_T;
+    ++n_contrib;
 }
 
 // --------------------------------------------------------------- forward
 template <int CD, bool PACK>
-__global__ void __launch_bounds__(1024) raster_fwd_kernel(RasterArgs a) {
+__global__ void __launch_bounds__(512) raster_fwd_kernel(RasterArgs a) {
     extern __shared__ __align__(128) unsigned char sm[];
-    const int B = blockDim.x;
-    const int nw = B >> 5;
-    const SmemLayout L = smem_layout<CD, PACK, false>(B);
+    const int NT = blockDim.x, nw = NT >> 5, BR = 2 * NT;
+    const SmemLayout L = smem_layout<CD, PACK, false>(NT);
     uint64_t *mbar = reinterpret_cast<uint64_t *>(sm);
     uint32_t *wmask = reinterpret_cast<uint32_t *>(sm + L.mask_off);
     GeoRec *srec = reinterpret_cast<GeoRec *>(sm + L.rec_off);
@@ -178,19 +234,22 @@ __global__ void __launch_bounds__(1024) raster_fwd_kernel(RasterArgs a) {
     const int tile = bt - cam * a.n_tiles;
     const int ty = tile / a.TW, tx = tile - ty * a.TW;
     const int wpr = a.TS >> 3;
-    const int i = ty * a.TS + (warp / wpr) * 4 + (lane >> 3);
     const int j = tx * a.TS + (warp % wpr) * 8 + (lane & 7);
-    const bool inside = (i < a.H) && (j < a.W);
-    const int64_t pix = ((int64_t)cam * a.H + i) * a.W + j;
+    const int i0 = ty * a.TS + (warp / wpr) * 8 + (lane >> 3) * 2;
+    const bool in0 = (i0 < a.H) && (j < a.W);
+    const bool in1 = (i0 + 1 < a.H) && (j < a.W);
+    const int64_t pix0 = ((int64_t)cam * a.H + i0) * a.W + j;
+    const int64_t pix1 = pix0 + a.W;
     const float *bg = a.bg ? a.bg + (int64_t)cam * CD : nullptr;
 
     if (a.masks && !a.masks[bt]) {
-        if (inside) {
 #pragma unroll
-            for (int k = 0; k < CD; ++k) a.out_c[pix * CD + k] = bg ? bg[k] : 0.f;
-            a.out_a[pix] = 0.f;
-            a.last_ids[pix] = 0;
+        for (int k = 0; k < CD; ++k) {
+            if (in0) a.out_c[pix0 * CD + k] = bg ? bg[k] : 0.f;
+            if (in1) a.out_c[pix1 * CD + k] = bg ? bg[k] : 0.f;
         }
+        if (in0) { a.out_a[pix0] = 0.f; a.last_ids[pix0] = 0; }
+        if (in1) { a.out_a[pix1] = 0.f; a.last_ids[pix1] = 0; }
         return;
     }
 
@@ -198,16 +257,16 @@ __global__ void __launch_bounds__(1024) raster_fwd_kernel(RasterArgs a) {
     int32_t re = (bt == a.C * a.n_tiles - 1) ? (int32_t)a.n_isects : a.offsets[bt + 1];
     rs = max(0, min(rs, (int32_t)a.n_isects));
     re = max(rs, min(re, (int32_t)a.n_isects));
-    const int nb = (re - rs + B - 1) / B;
+    const int nb = (re - rs + BR - 1) / BR;
 
-    const float px = (float)j + 0.5f, py = (float)i + 0.5f;
-    float T = 1.0f;
-    int32_t cur = 0;
+    const float px = (float)j + 0.5f, py0 = (float)i0 + 0.5f, py1 = py0 + 1.f;
+    float T0 = 1.0f, T1 = 1.0f;
+    int32_t cur0 = 0, cur1 = 0;
     uint32_t n_contrib = 0;
-    float acc[CD];
+    float acc0[CD], acc1[CD];
 #pragma unroll
-    for (int k = 0; k < CD; ++k) acc[k] = 0.f;
-    bool done = !inside;
+    for (int k = 0; k < CD; ++k) acc0[k] = acc1[k] = 0.f;
+    bool d0 = !in0, d1 = !in1;
 
     if (nb > 0) {
         if (tid == 0) {
@@ -218,82 +277,62 @@ __global__ void __launch_bounds__(1024) raster_fwd_kernel(RasterArgs a) {
         __syncthreads();
         int issued = 0, waited = 0;
         if (tid == 0) {
-            issue_batch<PACK>(a, srec, scol4, mbar, B, 0, rs, min(B, re - rs));
+            issue_batch<PACK>(a, srec, scol4, mbar, BR, 0, rs, min(BR, re - rs));
             issued = 1;
         }
         for (int b = 0; b < nb; ++b) {
-            const int32_t bs = rs + b * B;
-            const int cnt = min(B, re - bs);
+            const int32_t bs = rs + b * BR;
+            const int cnt = min(BR, re - bs);
             const int buf = b & 1;
             if (tid == 0 && b + 1 < nb) {
-                const int32_t bn = bs + B;
-                issue_batch<PACK>(a, srec, scol4, mbar, B, buf ^ 1, bn, min(B, re - bn));
+                const int32_t bn = bs + BR;
+                issue_batch<PACK>(a, srec, scol4, mbar, BR, buf ^ 1, bn, min(BR, re - bn));
                 issued = b + 2;
             }
             const bool ok = mbar_wait_bounded(&mbar[buf], (b >> 1) & 1);
             if (tid == 0 && ok) waited = b + 1;
-            const bool valid = tid < cnt;
-            GeoRec r;
-            if (valid) r = srec[buf * B + tid];
-            build_masks(r, valid, 0, nw, wpr, tx * a.TS, ty * a.TS, warp, lane, wmask, nullptr);
-            if (!PACK && valid) {
-                const float *cp = a.colors + (int64_t)r.gid * CD;
+            const GeoRec *batch = srec + buf * BR;
+            build_masks(batch, cnt, 0, NT, nw, wpr, tx * a.TS, ty * a.TS, tid, lane, wmask,
+                        nullptr);
+            if (!PACK) {
 #pragma unroll
-                for (int k = 0; k < CD; ++k) scol[(buf * B + tid) * CD + k] = cp[k];
+                for (int half = 0; half < 2; ++half) {
+                    const int s = tid + half * NT;
+                    if (s < cnt) {
+                        const float *cp = a.colors + (int64_t)batch[s].gid * CD;
+#pragma unroll
+                        for (int k = 0; k < CD; ++k) scol[(buf * BR + s) * CD + k] = cp[k];
+                    }
+                }
             }
             if (__syncthreads_or(!ok)) {
                 if (tid == 0) atomicOr(a.status, DEV_ERR_WAIT_TIMEOUT);
-                done = true;
+                d0 = d1 = true;
                 break;
             }
-            if (!__all_sync(0xffffffffu, done)) {
+            if (!__all_sync(0xffffffffu, d0 && d1)) {
                 bool warp_done = false;
-                for (int k = 0; k < nw && !warp_done; ++k) {
-                    uint32_t m = wmask[warp * nw + k];
+                for (int k = 0; k < 2 * nw && !warp_done; ++k) {
+                    uint32_t m = wmask[warp * 2 * nw + k];
                     while (m) {
                         const int bit = __ffs(m) - 1;
                         m &= m - 1;
                         const int t = k * 32 + bit;
-                        const GeoRec q = srec[buf * B + t];
-                        if (!done) {
-                            const float dx = q.x - px, dy = q.y - py;
-                            const float sigma =
-                                (q.cxx * dx * dx + q.cyy * dy * dy) + 2.f * q.cxy * dx * dy;
-                            if (!(sigma < 0.f || sigma >= 1.f)) {
-                                const float alpha =
-                                    fminf(0.999f, q.opac * __powf(1.f - sigma, q.beta));
-                                const float next_T = T * (1.f - alpha);
-                                if (next_T <= 1e-4f) {
-                                    done = true;
-                                } else {
-                                    const float vis = alpha * T;
-                                    if (PACK) {
-                                        const float4 c = scol4[buf * B + t];
-                                        acc[0] += c.x * vis;
-                                        if (CD > 1) acc[1 % CD] += c.y * vis;
-                                        if (CD > 2) acc[2 % CD] += c.z * vis;
-                                        if (CD > 3) acc[3 % CD] += c.w * vis;
-                                    } else {
-#pragma unroll
-                                        for (int k2 = 0; k2 < CD; ++k2)
-                                            acc[k2] += scol[(buf * B + t) * CD + k2] * vis;
-                                    }
-                                    cur = bs + t;
-                                    T = next_T;
-                                    ++n_contrib;
-                                }
-                            }
-                        }
-                        if (__all_sync(0xffffffffu, done)) {
+                        const GeoRec q = batch[t];
+                        float col[CD];
+                        load_color<CD, PACK>(scol4, scol, buf * BR + t, col);
+                        blend_one<CD>(q, col, px, py0, T0, acc0, cur0, d0, bs + t, n_contrib);
+                        blend_one<CD>(q, col, px, py1, T1, acc1, cur1, d1, bs + t, n_contrib);
+                        if (__all_sync(0xffffffffu, d0 && d1)) {
                             warp_done = true;
                             break;
                         }
                     }
                 }
             }
-            if (__syncthreads_count(done) == B) break;
+            if (__syncthreads_count(d0 && d1) == NT) break;
         }
-        // make sure no bulk copy still targets this CTA's shared memory
+        // no bulk copy may still target this CTA's shared memory at exit
         if (tid == 0)
             for (int b = waited; b < issued; ++b)
                 if (!mbar_wait_bounded(&mbar[b & 1], (b >> 1) & 1))
@@ -304,26 +343,118 @@ __global__ void __launch_bounds__(1024) raster_fwd_kernel(RasterArgs a) {
         const uint32_t w = __reduce_add_sync(0xffffffffu, n_contrib);
         if (lane == 0 && w) atomicAdd(a.pair_count, (unsigned long long)w);
     }
-    if (inside) {
-        a.out_a[pix] = 1.0f - T;
+    if (in0) {
+        a.out_a[pix0] = 1.0f - T0;
 #pragma unroll
-        for (int k = 0; k < CD; ++k) a.out_c[pix * CD + k] = bg ? acc[k] + T * bg[k] : acc[k];
-        a.last_ids[pix] = cur;
+        for (int k = 0; k < CD; ++k) a.out_c[pix0 * CD + k] = bg ? acc0[k] + T0 * bg[k] : acc0[k];
+        a.last_ids[pix0] = cur0;
+    }
+    if (in1) {
+        a.out_a[pix1] = 1.0f - T1;
+#pragma unroll
+        for (int k = 0; k < CD; ++k) a.out_c[pix1 * CD + k] = bg ? acc1[k] + T1 * bg[k] : acc1[k];
+        a.last_ids[pix1] = cur1;
     }
 }
 
 // -------------------------------------------------------------- backward
+// Per-pixel state of the back-to-front pass.  The reference keeps the colour
+// accumulated behind the current record per channel (buf_k) and forms
+// sum_k (c_k T - buf_k ra) v_k + T_final ra (v_a - bg.v); only the scalar
+// S = sum_k buf_k v_k enters, so it is carried instead of buf, and
+// K = T_final (v_a - bg.v) is folded once per pixel.
+template <int CD> struct BwdPix {
+    float T, S, K;
+    float vrc[CD];
+    int32_t bin;
+    bool inside;
+};
+
+template <int CD>
+__device__ __forceinline__ void bwd_pix_init(BwdPix<CD> &s, const RasterArgs &a, int64_t pix,
+                                             bool inside, const float *bg) {
+    s.inside = inside;
+    const float T_final = 1.0f - a.render_alphas[pix];
+    s.T = T_final;
+    s.bin = inside ? a.last_in[pix] : 0;
+    float bgdot = 0.f;
+#pragma unroll
+    for (int k = 0; k < CD; ++k) {
+        s.vrc[k] = a.v_out_c[pix * CD + k];
+        if (bg) bgdot += bg[k] * s.vrc[k];
+    }
+    s.K = T_final * (a.v_out_a[pix] - bgdot);
+    s.S = 0.f;
+}
+
+// One back-to-front step of one pixel (rasterize_to_pixels_bwd.cu:158-247); adds
+// the pixel's gradient contributions into g = [v_xy(2), v_conic(3), v_opacity,
+// v_beta, v_color(CD)].  (1-sigma)^(beta-1) and ln(1-sigma) are formed from
+// (1-sigma)^beta and one base-2 logarithm.
+template <int CD>
+__device__ __forceinline__ bool grad_one(const GeoRec &q, const float (&col)[CD], float px,
+                                         float py, int32_t idx, BwdPix<CD> &s,
+                                         float (&g)[7 + CD]) {
+    if (!s.inside || idx > s.bin) return false;
+    const float dx = q.x - px, dy = q.y - py;
+    const float sigma = (q.cxx * dx * dx + q.cyy * dy * dy) + 2.f * q.cxy * dx * dy;
+    if (sigma < 0.f || sigma >= 1.f) return false;
+    const float om = 1.f - sigma;
+    const float vis = __powf(om, q.beta);
+    const float alpha = fminf(0.999f, q.opac * vis);
+    const float ra = 1.0f / (1.0f - alpha);
+    s.T *= ra;
+    const float fac = alpha * s.T;
+    float cv = 0.f;
+#pragma unroll
+    for (int k = 0; k < CD; ++k) {
+        g[7 + k] += fac * s.vrc[k];
+        cv += col[k] * s.vrc[k];
+    }
+    const float v_alpha = s.T * cv + ra * (s.K - s.S);
+    if (q.opac * vis <= 0.999f) {
+        const float v_sigma = -v_alpha * q.opac * q.beta * __fdividef(vis, om);
+        g[2] += dx * dx * v_sigma;
+        g[3] += 2.f * dx * dy * v_sigma;
+        g[4] += dy * dy * v_sigma;
+        g[0] += 2.f * v_sigma * (q.cxx * dx + q.cxy * dy);
+        g[1] += 2.f * v_sigma * (q.cxy * dx + q.cyy * dy);
+        g[5] += vis * v_alpha;
+        g[6] += v_alpha * q.opac * vis * (__log2f(om) * 0.6931471805599453f);
+    }
+    s.S += fac * cv;
+    return true;
+}
+
+// Sums g[OFF .. OFF+REM) over the warp in power-of-two chunks and adds each
+// total once into the record's shared accumulator.
+template <int OFF, int REM> struct ReduceChunks {
+    template <int NV>
+    static __device__ __forceinline__ void run(const float (&g)[NV], int lane, float *acc) {
+        constexpr int S = REM >= 32 ? 32 : REM >= 16 ? 16 : REM >= 8 ? 8 : REM >= 4 ? 4
+                                                                         : REM >= 2 ? 2 : 1;
+        float v[S];
+#pragma unroll
+        for (int i = 0; i < S; ++i) v[i] = g[OFF + i];
+        const float tot = tr_reduce<S>(v, lane);
+        if ((lane & (32 / S - 1)) == 0 && tot != 0.f) atomicAdd(&acc[OFF + tr_index<S>(lane)], tot);
+        ReduceChunks<OFF + S, REM - S>::run(g, lane, acc);
+    }
+};
+template <int OFF> struct ReduceChunks<OFF, 0> {
+    template <int NV>
+    static __device__ __forceinline__ void run(const float (&)[NV], int, float *) {}
+};
+
 template <int CD, bool PACK>
-__global__ void __launch_bounds__(1024) raster_bwd_kernel(RasterArgs a) {
+__global__ void __launch_bounds__(512) raster_bwd_kernel(RasterArgs a) {
     constexpr int NV = 7 + CD;
-    constexpr int NG = (NV + 15) / 16;
     extern __shared__ __align__(128) unsigned char sm[];
-    const int B = blockDim.x;
-    const int nw = B >> 5;
-    const SmemLayout L = smem_layout<CD, PACK, true>(B);
+    const int NT = blockDim.x, nw = NT >> 5, BR = 2 * NT;
+    const SmemLayout L = smem_layout<CD, PACK, true>(NT);
     uint64_t *mbar = reinterpret_cast<uint64_t *>(sm);
     uint32_t *wmask = reinterpret_cast<uint32_t *>(sm + L.mask_off);
-    int32_t *wbin = reinterpret_cast<int32_t *>(sm + L.mask_off + nw * nw * 4);
+    int32_t *wbin = reinterpret_cast<int32_t *>(sm + L.mask_off + nw * 2 * nw * 4);
     GeoRec *srec = reinterpret_cast<GeoRec *>(sm + L.rec_off);
     float4 *scol4 = reinterpret_cast<float4 *>(sm + L.col_off);
     float *scol = reinterpret_cast<float *>(sm + L.col_off);
@@ -337,12 +468,15 @@ __global__ void __launch_bounds__(1024) raster_bwd_kernel(RasterArgs a) {
     const int tile = bt - cam * a.n_tiles;
     const int ty = tile / a.TW, tx = tile - ty * a.TW;
     const int wpr = a.TS >> 3;
-    const int i = ty * a.TS + (warp / wpr) * 4 + (lane >> 3);
     const int j = tx * a.TS + (warp % wpr) * 8 + (lane & 7);
-    const bool inside = (i < a.H) && (j < a.W);
-    // outside threads read a clamped pixel, like the reference, and never contribute
-    const int64_t pix_in = min((int64_t)i * a.W + j, (int64_t)a.W * a.H - 1);
-    const int64_t pix = (int64_t)cam * a.H * a.W + pix_in;
+    const int i0 = ty * a.TS + (warp / wpr) * 8 + (lane >> 3) * 2;
+    const bool in0 = (i0 < a.H) && (j < a.W);
+    const bool in1 = (i0 + 1 < a.H) && (j < a.W);
+    // outside pixels read a clamped pixel, like the reference, and never contribute
+    const int64_t img = (int64_t)a.W * a.H;
+    const int64_t base = (int64_t)cam * img;
+    const int64_t pix0 = base + min((int64_t)i0 * a.W + j, img - 1);
+    const int64_t pix1 = base + min((int64_t)(i0 + 1) * a.W + j, img - 1);
     const float *bg = a.bg ? a.bg + (int64_t)cam * CD : nullptr;
 
     int32_t rs = a.offsets[bt];
@@ -350,28 +484,16 @@ __global__ void __launch_bounds__(1024) raster_bwd_kernel(RasterArgs a) {
     rs = max(0, min(rs, (int32_t)a.n_isects));
     re = max(rs, min(re, (int32_t)a.n_isects));
 
-    const float px = (float)j + 0.5f, py = (float)i + 0.5f;
-    const float T_final = 1.0f - a.render_alphas[pix];
-    float T = T_final;
-    const int32_t bin_final = inside ? a.last_in[pix] : 0;
-    float vrc[CD], buf_c[CD];
-#pragma unroll
-    for (int k = 0; k < CD; ++k) {
-        vrc[k] = a.v_out_c[pix * CD + k];
-        buf_c[k] = 0.f;
-    }
-    const float vra = a.v_out_a[pix];
-    float bgdot = 0.f;
-    if (bg) {
-#pragma unroll
-        for (int k = 0; k < CD; ++k) bgdot += bg[k] * vrc[k];
-    }
+    const float px = (float)j + 0.5f, py0 = (float)i0 + 0.5f, py1 = py0 + 1.f;
+    BwdPix<CD> s0, s1;
+    bwd_pix_init<CD>(s0, a, pix0, in0, bg);
+    bwd_pix_init<CD>(s1, a, pix1, in1, bg);
 
-    // warp- and block-level bounds on the last contributor index
-    const int32_t wb = __reduce_max_sync(0xffffffffu, inside ? bin_final : INT32_MIN);
+    const int32_t wb = __reduce_max_sync(
+        0xffffffffu, max(in0 ? s0.bin : INT32_MIN, in1 ? s1.bin : INT32_MIN));
     if (lane == 0) wbin[warp] = wb;
-    for (int t = tid; t < B * NG * 16; t += B) gacc[t] = 0.f;
-    touched[tid] = 0;
+    for (int t = tid; t < BR * NV; t += NT) gacc[t] = 0.f;
+    for (int t = tid; t < BR; t += NT) touched[t] = 0;
     if (tid == 0) {
         mbar_init(&mbar[0], 1);
         mbar_init(&mbar[1], 1);
@@ -381,136 +503,89 @@ __global__ void __launch_bounds__(1024) raster_bwd_kernel(RasterArgs a) {
     int32_t block_bin = INT32_MIN;
     for (int w = 0; w < nw; ++w) block_bin = max(block_bin, wbin[w]);
     const int32_t hi_end = max(rs, min(re, block_bin + 1)); // exclusive upper index
-    const int nb = (hi_end - rs + B - 1) / B;
+    const int nb = (hi_end - rs + BR - 1) / BR;
 
     int issued = 0, waited = 0;
     if (nb > 0 && tid == 0) {
-        const int32_t lo = max(rs, hi_end - B);
-        issue_batch<PACK>(a, srec, scol4, mbar, B, 0, lo, hi_end - lo);
+        const int32_t lo = max(rs, hi_end - BR);
+        issue_batch<PACK>(a, srec, scol4, mbar, BR, 0, lo, hi_end - lo);
         issued = 1;
     }
     for (int b = 0; b < nb; ++b) {
-        const int32_t hi = hi_end - b * B;
-        const int32_t lo = max(rs, hi - B);
+        const int32_t hi = hi_end - b * BR;
+        const int32_t lo = max(rs, hi - BR);
         const int cnt = hi - lo;
         const int buf = b & 1;
         if (tid == 0 && b + 1 < nb) {
-            const int32_t hn = hi - B;
-            const int32_t ln = max(rs, hn - B);
-            issue_batch<PACK>(a, srec, scol4, mbar, B, buf ^ 1, ln, hn - ln);
+            const int32_t hn = hi - BR;
+            const int32_t ln = max(rs, hn - BR);
+            issue_batch<PACK>(a, srec, scol4, mbar, BR, buf ^ 1, ln, hn - ln);
             issued = b + 2;
         }
         const bool ok = mbar_wait_bounded(&mbar[buf], (b >> 1) & 1);
         if (tid == 0 && ok) waited = b + 1;
-        const bool valid = tid < cnt;
-        GeoRec r;
-        int32_t my_gid = 0;
-        if (valid) {
-            r = srec[buf * B + tid];
-            my_gid = r.gid;
-        }
-        build_masks(r, valid, lo + tid, nw, wpr, tx * a.TS, ty * a.TS, warp, lane, wmask, wbin);
-        if (!PACK && valid) {
-            const float *cp = a.colors + (int64_t)my_gid * CD;
+        const GeoRec *batch = srec + buf * BR;
+        const int32_t gid0 = (tid < cnt) ? batch[tid].gid : 0;
+        const int32_t gid1 = (tid + NT < cnt) ? batch[tid + NT].gid : 0;
+        build_masks(batch, cnt, lo, NT, nw, wpr, tx * a.TS, ty * a.TS, tid, lane, wmask, wbin);
+        if (!PACK) {
 #pragma unroll
-            for (int k = 0; k < CD; ++k) scol[(buf * B + tid) * CD + k] = cp[k];
+            for (int half = 0; half < 2; ++half) {
+                const int sl = tid + half * NT;
+                if (sl < cnt) {
+                    const float *cp = a.colors + (int64_t)(half ? gid1 : gid0) * CD;
+#pragma unroll
+                    for (int k = 0; k < CD; ++k) scol[(buf * BR + sl) * CD + k] = cp[k];
+                }
+            }
         }
         if (__syncthreads_or(!ok)) {
             if (tid == 0) atomicOr(a.status, DEV_ERR_WAIT_TIMEOUT);
             break;
         }
-        for (int k = nw - 1; k >= 0; --k) {
-            uint32_t m = wmask[warp * nw + k];
+        for (int k = 2 * nw - 1; k >= 0; --k) {
+            uint32_t m = wmask[warp * 2 * nw + k];
             while (m) {
                 const int bit = 31 - __clz(m);
                 m &= ~(1u << bit);
                 const int t = k * 32 + bit;
                 const int32_t idx = lo + t;
-                const GeoRec q = srec[buf * B + t];
-                bool v = inside && (idx <= bin_final);
-                float dx = 0.f, dy = 0.f, sigma = 0.f, vis = 0.f, alpha = 0.f;
-                if (v) {
-                    dx = q.x - px;
-                    dy = q.y - py;
-                    sigma = (q.cxx * dx * dx + q.cyy * dy * dy) + 2.f * q.cxy * dx * dy;
-                    if (sigma < 0.f || sigma >= 1.f) v = false;
-                    vis = __powf(1.f - sigma, q.beta);
-                    alpha = fminf(0.999f, q.opac * vis);
-                }
-                if (!__any_sync(0xffffffffu, v)) continue;
-                float g[NG * 16];
+                const GeoRec q = batch[t];
+                float col[CD];
+                load_color<CD, PACK>(scol4, scol, buf * BR + t, col);
+                float g[NV];
 #pragma unroll
-                for (int u = 0; u < NG * 16; ++u) g[u] = 0.f;
-                if (v) {
-                    float col[CD];
-                    if (PACK) {
-                        const float4 c = scol4[buf * B + t];
-                        col[0] = c.x;
-                        if (CD > 1) col[1 % CD] = c.y;
-                        if (CD > 2) col[2 % CD] = c.z;
-                        if (CD > 3) col[3 % CD] = c.w;
-                    } else {
-#pragma unroll
-                        for (int k2 = 0; k2 < CD; ++k2) col[k2] = scol[(buf * B + t) * CD + k2];
-                    }
-                    const float ra = 1.0f / (1.0f - alpha);
-                    T *= ra;
-                    const float fac = alpha * T;
-                    float v_alpha = 0.f;
-#pragma unroll
-                    for (int k2 = 0; k2 < CD; ++k2) {
-                        g[7 + k2] = fac * vrc[k2];
-                        v_alpha += (col[k2] * T - buf_c[k2] * ra) * vrc[k2];
-                    }
-                    v_alpha += T_final * ra * vra;
-                    if (bg) v_alpha += -T_final * ra * bgdot;
-                    if (q.opac * vis <= 0.999f) {
-                        const float v_sigma =
-                            -v_alpha * q.opac * q.beta * __powf(1.f - sigma, q.beta - 1.f);
-                        g[2] = dx * dx * v_sigma;
-                        g[3] = 2.f * dx * dy * v_sigma;
-                        g[4] = dy * dy * v_sigma;
-                        g[0] = 2.f * v_sigma * (q.cxx * dx + q.cxy * dy);
-                        g[1] = 2.f * v_sigma * (q.cxy * dx + q.cyy * dy);
-                        g[5] = vis * v_alpha;
-                        g[6] = v_alpha * q.opac * __powf(1.f - sigma, q.beta) *
-                               __logf(1.f - sigma);
-                    }
-#pragma unroll
-                    for (int k2 = 0; k2 < CD; ++k2) buf_c[k2] += col[k2] * fac;
-                }
-#pragma unroll
-                for (int grp = 0; grp < NG; ++grp) {
-                    float vv[16];
-#pragma unroll
-                    for (int u = 0; u < 16; ++u) vv[u] = g[grp * 16 + u];
-                    const float tot = warp_transpose_reduce16(vv, lane);
-                    const int vi = grp * 16 + transpose_reduce_index(lane);
-                    if (!(lane & 1) && vi < NV && tot != 0.f)
-                        atomicAdd(&gacc[t * NG * 16 + vi], tot);
-                }
+                for (int u = 0; u < NV; ++u) g[u] = 0.f;
+                bool any = grad_one<CD>(q, col, px, py0, idx, s0, g);
+                any |= grad_one<CD>(q, col, px, py1, idx, s1, g);
+                if (!__any_sync(0xffffffffu, any)) continue;
+                ReduceChunks<0, NV>::run(g, lane, gacc + t * NV);
                 if (lane == 0) touched[t] = 1;
             }
         }
         __syncthreads();
-        if (valid && touched[tid]) {
-            const int64_t gg = my_gid;
-            float *ga = gacc + tid * NG * 16;
 #pragma unroll
-            for (int u = 0; u < NV; ++u) {
-                const float val = ga[u];
-                if (val != 0.f) {
-                    float *dst;
-                    if (u < 2) dst = a.v_m2 + 2 * gg + u;
-                    else if (u < 5) dst = a.v_cn + 3 * gg + (u - 2);
-                    else if (u == 5) dst = a.v_op + gg;
-                    else if (u == 6) dst = a.v_be + gg;
-                    else dst = a.v_col + gg * CD + (u - 7);
-                    atomicAdd(dst, val);
+        for (int half = 0; half < 2; ++half) {
+            const int sl = tid + half * NT;
+            if (sl < cnt && touched[sl]) {
+                const int64_t gg = half ? gid1 : gid0;
+                float *ga = gacc + sl * NV;
+#pragma unroll
+                for (int u = 0; u < NV; ++u) {
+                    const float val = ga[u];
+                    if (val != 0.f) {
+                        float *dst;
+                        if (u < 2) dst = a.v_m2 + 2 * gg + u;
+                        else if (u < 5) dst = a.v_cn + 3 * gg + (u - 2);
+                        else if (u == 5) dst = a.v_op + gg;
+                        else if (u == 6) dst = a.v_be + gg;
+                        else dst = a.v_col + gg * CD + (u - 7);
+                        atomicAdd(dst, val);
+                    }
+                    ga[u] = 0.f;
                 }
-                ga[u] = 0.f;
+                touched[sl] = 0;
             }
-            touched[tid] = 0;
         }
     }
     if (tid == 0)
@@ -553,8 +628,8 @@ static int launch_pack(int64_t T, int64_t n_prims, const int32_t *fl, const floa
 template <int CD, bool BWD>
 static int launch_blend(RasterArgs &a, cudaStream_t st) {
     constexpr bool PACK = CD <= 4;
-    const int B = a.TS * a.TS;
-    const SmemLayout L = smem_layout<CD, PACK, BWD>(B);
+    const int NT = a.TS * a.TS / 2; // two pixels per thread
+    const SmemLayout L = smem_layout<CD, PACK, BWD>(NT);
     if (L.total > 227 * 1024)
         return set_error(UBS_ERR_UNSUPPORTED, "raster: tile_size %d with %d channels needs %d B "
                                               "of shared memory", a.TS, CD, L.total);
@@ -564,7 +639,7 @@ static int launch_blend(RasterArgs &a, cudaStream_t st) {
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total) !=
         cudaSuccess)
         return check_launch("raster smem attribute");
-    k<<<nblocks, B, L.total, st>>>(a);
+    k<<<nblocks, NT, L.total, st>>>(a);
     note_launch();
     return check_launch(BWD ? "raster_bwd" : "raster_fwd");
 }
