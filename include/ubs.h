@@ -212,6 +212,55 @@ int ubs_raster_bwd_packed(int32_t C, int64_t N, int32_t channels, int64_t n_isec
                           float *v_betas, int32_t zero_outputs, void *workspace,
                           size_t workspace_bytes, void *stream);
 
+/* ------------------------------------------------------- fused multi-view ---
+ * One render of a Universal Beta Splatting scene into C views at once (no
+ * single reference counterpart: it fuses the reference model's render,
+ * scene/beta_model.py:660-722, with rasterization(), rendering.py:17-232).
+ * Raw (pre-activation) parameters as the reference model stores them: xyz
+ * [N,3], mean [N,dim-3], scale [N,dim] (softplus), l_triangle
+ * [N,dim*(dim-1)/2] (first 3 = rotation skew, rest = strictly-lower entries of
+ * rows 3..dim-1, row-major), opacity [N] (sigmoid), beta [N,dim-2] (4 exp;
+ * beta[:,0] spatial), rgb [N,3]; dim in {6, 7}.
+ * Views: viewmats [C,16] world-to-camera row-major, intrinsics [C,4]
+ * (fx, fy, cx, cy), centers [C,3] camera centres, timestamps [C] (dim 7; may be
+ * NULL for dim 6), view_dims [C,4] (width, height, tile columns, tile rows),
+ * tile_base [C+1] (first (view, tile) bucket of each view; tile_base[C] =
+ * n_buckets), pix_base [C+1] (first pixel of each view).  Images are one flat
+ * buffer: render_colors [P,3], render_alphas [P], last_ids [P], P = pix_base[C].
+ * backgrounds [C,3] or NULL.  `capacity` bounds the number of intersections
+ * held in the workspace (ubs_scene_workspace_bytes); a frame that needs more
+ * sets status bit 4 (read with ubs_scene_stats) and must be re-rendered with a
+ * larger capacity.  No host synchronisation: both calls can be captured in a
+ * CUDA graph.  The backward uses the workspace of the forward it follows and
+ * overwrites the raw-parameter gradients (summed over views). */
+size_t ubs_scene_workspace_bytes(int32_t C, int64_t N, int32_t n_buckets, int64_t capacity);
+int ubs_scene_forward(int32_t dim, int64_t N, const float *xyz, const float *mean,
+                      const float *scale, const float *l_triangle, const float *opacity,
+                      const float *beta, const float *rgb, int32_t C, const float *viewmats,
+                      const float *intrinsics, const float *centers, const float *timestamps,
+                      const int32_t *view_dims, const int32_t *tile_base,
+                      const int64_t *pix_base, int32_t n_buckets, int32_t tile_size,
+                      float eps2d, float near_plane, float far_plane, float radius_clip,
+                      const float *backgrounds, float *render_colors, float *render_alphas,
+                      int32_t *last_ids, int64_t capacity, void *workspace,
+                      size_t workspace_bytes, void *stream);
+int ubs_scene_backward(int32_t dim, int64_t N, const float *xyz, const float *mean,
+                       const float *scale, const float *l_triangle, const float *opacity,
+                       const float *beta, const float *rgb, int32_t C, const float *viewmats,
+                       const float *intrinsics, const float *centers, const float *timestamps,
+                       const int32_t *view_dims, const int32_t *tile_base,
+                       const int64_t *pix_base, int32_t n_buckets, int32_t tile_size,
+                       float eps2d, float near_plane, float far_plane, float radius_clip,
+                       const float *backgrounds, const float *render_alphas,
+                       const int32_t *last_ids, const float *v_render_colors,
+                       const float *v_render_alphas, float *v_xyz, float *v_mean, float *v_scale,
+                       float *v_l_triangle, float *v_opacity, float *v_beta, float *v_rgb,
+                       int32_t exact_cond_grad, int64_t capacity, void *workspace,
+                       size_t workspace_bytes, void *stream);
+/* Intersections counted by the last forward on `workspace` and its device
+ * status word; synchronises the stream. */
+int ubs_scene_stats(const void *workspace, int64_t *n_isects, uint32_t *status, void *stream);
+
 /* Device status word (bits: 1 wait timeout, 2 negative depth, 4 overflow,
  * 8 bad flatten index) and the contributing-pair count of the last packed
  * blend on `workspace` (pair_count may be NULL); synchronises the stream. */

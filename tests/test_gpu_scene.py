@@ -1,0 +1,121 @@
+"""The fused multi-view render (ubs.render) against the drop-in operator
+sequence of the reference model's render (ubs.scene.render_view, which calls
+the gsplat-compatible operators one by one) on the same scenes.
+
+Both paths evaluate the same mathematics with different kernel fusion and
+summation order, so images agree to FP32 rounding (1e-5 max abs) and
+gradients to 1e-4 relative (L2 per parameter tensor)."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from ubs import scene as S
+from ubs.render import Renderer, Views
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+
+
+def rel_l2(a, b):
+    a, b = a.detach().double(), b.detach().double()
+    return float((a - b).norm() / b.norm().clamp_min(1e-30))
+
+
+def make_params(N, D, seed, xyz_range=1.0):
+    p = S.synthetic_params(N, D, seed=seed, xyz_range=xyz_range, device=DEV)
+    # larger spatial scales than the benchmark so small images get dense coverage
+    p["scale"][:, :3] += 1.5
+    return p
+
+
+def dropin_render(p, cam, bg, exact=False):
+    from gsplat.cuda import _wrapper as Wr
+    ri, rj = S.rest_indices(p["scale"].shape[1], DEV)
+    leaves = {k: v.detach().clone().requires_grad_(True) for k, v in p.items()}
+    prev = Wr.get_cond_grad_mode()
+    Wr.set_cond_grad_mode("exact" if exact else "reference")
+    try:
+        img, alphas, _ = S.render_view(leaves, cam, bg, ri, rj)
+    finally:
+        Wr.set_cond_grad_mode(prev)
+    return img.permute(1, 2, 0), alphas[0, ..., 0], leaves
+
+
+def fused_render(p, cams, bg, exact=False, capacity=None):
+    r = Renderer(dim=p["scale"].shape[1], capacity=capacity, exact_cond_grad=exact)
+    views = Views(cams, device=DEV)
+    leaves = {k: v.detach().clone().requires_grad_(True) for k, v in p.items()}
+    colors, alphas = r.render(leaves, views, bg)
+    return r, views, colors, alphas, leaves
+
+
+@pytest.mark.parametrize("D,exact", [(6, False), (6, True), (7, False)])
+def test_fused_single_view_matches_dropin(D, exact):
+    p = make_params(6000, D, seed=D)
+    cam = S.orbit_view(5, 3.0, 320, 240, 280.0, 280.0, timestamp=0.37, device=DEV)
+    bg = torch.tensor([0.1, 0.2, 0.3], device=DEV)
+    img_d, alpha_d, leaves_d = dropin_render(p, cam, bg, exact)
+    _, views, colors, alphas, leaves_f = fused_render(p, [cam], bg, exact)
+    img_f = views.split(colors)[0]
+    assert float((img_f - img_d).detach().abs().max()) < 1e-5
+    assert float((alphas.view(240, 320) - alpha_d).abs().max()) < 1e-5
+    assert float(alpha_d.mean()) > 0.05  # the scene covers the image
+    g = torch.Generator().manual_seed(3)
+    w = torch.randn(240, 320, 3, generator=g).to(DEV)
+    wa = torch.randn(240, 320, generator=g).to(DEV)
+    ((img_d * w).sum() + (alpha_d * wa).sum()).backward()
+    ((img_f * w).sum() + (alphas.view(240, 320) * wa).sum()).backward()
+    for k in leaves_d:
+        assert rel_l2(leaves_f[k].grad, leaves_d[k].grad) < 1e-4, (k, rel_l2(leaves_f[k].grad,
+                                                                         leaves_d[k].grad))
+
+
+def test_fused_multiview_mixed_resolution():
+    p = make_params(5000, 6, seed=11)
+    cams = [S.orbit_view(1, 3.0, 160, 120, 150.0, 150.0, device=DEV),
+            S.orbit_view(2, 3.5, 200, 96, 170.0, 170.0, device=DEV),
+            S.orbit_view(3, 2.8, 96, 96, 90.0, 90.0, device=DEV)]
+    bgs = torch.rand(3, 3, generator=torch.Generator().manual_seed(0)).to(DEV)
+    _, views, colors, alphas, leaves_f = fused_render(p, cams, bgs)
+    imgs = views.split(colors)
+    g = torch.Generator().manual_seed(5)
+    ws = [torch.randn(c.height, c.width, 3, generator=g).to(DEV) for c in cams]
+    total_f = sum((im * w).sum() for im, w in zip(imgs, ws))
+    total_f.backward()
+    grads = {k: torch.zeros_like(v) for k, v in p.items()}
+    for v, cam in enumerate(cams):
+        img_d, _, leaves_d = dropin_render(p, cam, bgs[v])
+        assert float((imgs[v] - img_d).abs().max()) < 1e-5, v
+        (img_d * ws[v]).sum().backward()
+        for k in grads:
+            grads[k] += leaves_d[k].grad
+    for k in grads:
+        assert rel_l2(leaves_f[k].grad, grads[k]) < 1e-4, (k, rel_l2(leaves_f[k].grad, grads[k]))
+
+
+def test_fused_capacity_overflow_is_recovered():
+    p = make_params(4000, 6, seed=21)
+    cam = S.orbit_view(7, 3.0, 256, 192, 220.0, 220.0, device=DEV)
+    bg = torch.zeros(3, device=DEV)
+    r, views, colors, _, _ = fused_render(p, [cam], bg, capacity=1000)
+    assert r.last_isects > 1000 and r.capacity > r.last_isects
+    img_d, _, _ = dropin_render(p, cam, bg)
+    assert float((views.split(colors)[0] - img_d).abs().max()) < 1e-5
+
+
+def test_fused_unchecked_overflow_is_reported():
+    p = make_params(3000, 6, seed=22)
+    cam = S.orbit_view(8, 3.0, 200, 150, 180.0, 180.0, device=DEV)
+    r = Renderer(dim=6, capacity=500)
+    views = Views([cam], device=DEV)
+    with torch.no_grad():
+        r.render(p, views, check=False)
+        with pytest.raises(RuntimeError, match="capacity"):
+            r.render(p, views, check=False)
+    assert r.capacity > 500
+    with torch.no_grad():
+        colors, _ = r.render(p, views, check=True)
+    img_d, _, _ = dropin_render(p, cam, torch.zeros(3, device=DEV))
+    assert float((views.split(colors)[0] - img_d).abs().max()) < 1e-5

@@ -19,17 +19,9 @@
 // reference's stable radix sort, independent of scatter order.
 #include <algorithm>
 
-#include "ubs_common.cuh"
+#include "sort_common.cuh"
 
 namespace ubs {
-
-constexpr int SCAN_ITEMS = 4;
-constexpr int SCAN_THREADS = 1024;
-constexpr int SCAN_TILE = SCAN_ITEMS * SCAN_THREADS;
-constexpr int SMALL_SEG = 4096;       // largest bucket sorted in shared memory
-constexpr int SORT_THREADS = 256;
-constexpr int BIG_THREADS = 1024;
-constexpr int MERGE_ITEMS = 8;
 
 struct IsectHeader {
     int64_t total;     // number of intersections
@@ -49,8 +41,6 @@ static uint32_t bit_width_u32(uint32_t v) {
 }
 
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
-
-__host__ __device__ __forceinline__ int64_t imin64(int64_t a, int64_t b) { return a < b ? a : b; }
 
 struct CountWs {
     IsectHeader *hdr;
@@ -143,115 +133,6 @@ __global__ void isect_count_kernel(int64_t CN, int64_t N, const float2 *__restri
         for (uint32_t x = b.x0; x < b.x1; ++x) atomicAdd(&bc[y * tw + x], 1);
 }
 
-// ------------------------------------------------------------------- scan
-// Exclusive scan of int32 counts.  Per block: SCAN_TILE items; block-local
-// prefixes go to out, block totals to block_sums; a single block scans the
-// totals, a last pass adds them.  OutT is int32_t or int64_t.
-template <typename OutT>
-__global__ void __launch_bounds__(SCAN_THREADS) scan_blocks_kernel(const int32_t *__restrict__ in,
-                                                                  OutT *__restrict__ out,
-                                                                  int64_t n,
-                                                                  int64_t *__restrict__ sums) {
-    __shared__ int64_t warp_tot[32];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)tid * SCAN_ITEMS;
-    int64_t v[SCAN_ITEMS];
-    int64_t run = 0;
-#pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; ++k) {
-        const int64_t x = (base + k < n) ? (int64_t)in[base + k] : 0;
-        v[k] = run;
-        run += x;
-    }
-    // inclusive warp scan of thread totals
-    int64_t inc = run;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int64_t y = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += y;
-    }
-    if (lane == 31) warp_tot[warp] = inc;
-    __syncthreads();
-    if (warp == 0) {
-        int64_t w = warp_tot[lane];
-        int64_t wi = w;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int64_t y = __shfl_up_sync(0xffffffffu, wi, o);
-            if (lane >= o) wi += y;
-        }
-        warp_tot[lane] = wi - w; // exclusive
-        if (lane == 31) sums[blockIdx.x] = wi;
-    }
-    __syncthreads();
-    const int64_t off = warp_tot[warp] + (inc - run);
-#pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; ++k)
-        if (base + k < n) out[base + k] = (OutT)(v[k] + off);
-}
-
-__global__ void __launch_bounds__(SCAN_THREADS) scan_sums_kernel(int64_t *sums, int64_t nblocks,
-                                                                 int64_t *total) {
-    __shared__ int64_t warp_tot[32];
-    __shared__ int64_t carry;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) carry = 0;
-    __syncthreads();
-    for (int64_t base = 0; base < nblocks; base += SCAN_THREADS) {
-        const int64_t i = base + tid;
-        const int64_t x = i < nblocks ? sums[i] : 0;
-        int64_t inc = x;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int64_t y = __shfl_up_sync(0xffffffffu, inc, o);
-            if (lane >= o) inc += y;
-        }
-        if (lane == 31) warp_tot[warp] = inc;
-        __syncthreads();
-        if (warp == 0) {
-            const int64_t w = warp_tot[lane];
-            int64_t wi = w;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int64_t y = __shfl_up_sync(0xffffffffu, wi, o);
-                if (lane >= o) wi += y;
-            }
-            warp_tot[lane] = wi - w;
-        }
-        __syncthreads();
-        const int64_t c0 = carry;
-        if (i < nblocks) sums[i] = c0 + warp_tot[warp] + inc - x;
-        __syncthreads();
-        if (tid == SCAN_THREADS - 1) carry = c0 + warp_tot[warp] + inc;
-        __syncthreads();
-    }
-    if (tid == 0) *total = carry;
-}
-
-template <typename OutT>
-__global__ void scan_add_kernel(OutT *out, int64_t n, const int64_t *__restrict__ sums) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    out[i] = (OutT)((int64_t)out[i] + sums[i / SCAN_TILE]);
-}
-
-template <typename OutT>
-static int device_exclusive_scan(const int32_t *in, OutT *out, int64_t n, int64_t *sums,
-                                 int64_t *total, cudaStream_t st) {
-    if (n == 0) {
-        if (cudaMemsetAsync(total, 0, 8, st) != cudaSuccess) return check_launch("scan memset");
-        return UBS_OK;
-    }
-    const int64_t nblocks = (n + SCAN_TILE - 1) / SCAN_TILE;
-    scan_blocks_kernel<OutT><<<(unsigned)nblocks, SCAN_THREADS, 0, st>>>(in, out, n, sums);
-    ::ubs::note_launch();
-    scan_sums_kernel<<<1, SCAN_THREADS, 0, st>>>(sums, nblocks, total);
-    ::ubs::note_launch();
-    if (nblocks > 1) scan_add_kernel<OutT><<<grid_for(n, 256), 256, 0, st>>>(out, n, sums);
-    ::ubs::note_launch();
-    return check_launch("exclusive scan");
-}
-
 // ------------------------------------------------------------------- emit
 __global__ void isect_emit_bucket_kernel(int64_t CN, int64_t N, const float2 *__restrict__ means2d,
                                          const int32_t *__restrict__ radii,
@@ -307,122 +188,20 @@ __global__ void isect_emit_ordered_kernel(int64_t CN, int64_t N, const float2 *_
         }
 }
 
-// ------------------------------------------------------------ bucket sort
-__device__ __forceinline__ void write_sorted(uint64_t key, int64_t pos, int64_t cam,
-                                             int64_t tile, uint32_t tile_bits,
-                                             int64_t *isect_ids, int32_t *flatten_ids) {
-    const int32_t dbits = (int32_t)(key >> 32);
-    isect_ids[pos] = (cam << (32 + tile_bits)) | (tile << 32) | (int64_t)dbits;
-    flatten_ids[pos] = (int32_t)(key & 0xffffffffu);
-}
-
-// In-place bitonic sort of s[0..n2) (n2 a power of two) by the whole CTA.
-__device__ void block_bitonic(uint64_t *s, int n2) {
-    for (int k = 2; k <= n2; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = threadIdx.x; i < n2; i += blockDim.x) {
-                const int ixj = i ^ j;
-                if (ixj > i) {
-                    const uint64_t a = s[i], b = s[ixj];
-                    const bool up = (i & k) == 0;
-                    if ((a > b) == up) {
-                        s[i] = b;
-                        s[ixj] = a;
-                    }
-                }
-            }
-            __syncthreads();
-        }
+// Sorted-entry writer of the drop-in operator: isect_ids (camera | tile |
+// depth bits, the reference's key) and flatten_ids.
+struct IdsWriter {
+    int64_t *isect_ids;
+    int32_t *flatten_ids;
+    int32_t n_tiles;
+    uint32_t tile_bits;
+    __device__ __forceinline__ void operator()(uint64_t key, int64_t pos, int64_t bkt) const {
+        const int64_t cam = bkt / n_tiles, tile = bkt - cam * n_tiles;
+        const int32_t dbits = (int32_t)(key >> 32);
+        isect_ids[pos] = (cam << (32 + tile_bits)) | (tile << 32) | (int64_t)dbits;
+        flatten_ids[pos] = (int32_t)(key & 0xffffffffu);
     }
-}
-
-__global__ void __launch_bounds__(SORT_THREADS) bucket_sort_small_kernel(
-    int64_t n_buckets, int32_t n_tiles, uint32_t tile_bits, const int32_t *__restrict__ offsets,
-    int64_t T, const uint64_t *__restrict__ keys, int64_t *__restrict__ isect_ids,
-    int32_t *__restrict__ flatten_ids, int32_t *big_list, IsectHeader *hdr) {
-    __shared__ uint64_t s[SMALL_SEG];
-    const int64_t bkt = blockIdx.x;
-    const int64_t lo = offsets[bkt];
-    const int64_t hi = (bkt + 1 < n_buckets) ? (int64_t)offsets[bkt + 1] : T;
-    const int n = (int)(hi - lo);
-    if (n <= 0) return;
-    if (n > SMALL_SEG) {
-        if (threadIdx.x == 0) big_list[atomicAdd(&hdr->n_big, 1)] = (int32_t)bkt;
-        return;
-    }
-    int n2 = 1;
-    while (n2 < n) n2 <<= 1;
-    for (int i = threadIdx.x; i < n2; i += blockDim.x) s[i] = i < n ? keys[lo + i] : ~0ull;
-    __syncthreads();
-    block_bitonic(s, n2);
-    const int64_t cam = bkt / n_tiles, tile = bkt - cam * n_tiles;
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-        write_sorted(s[i], lo + i, cam, tile, tile_bits, isect_ids, flatten_ids);
-}
-
-// merge path: number of elements taken from a for output diagonal d
-__device__ __forceinline__ int64_t merge_split(const uint64_t *a, int64_t na, const uint64_t *b,
-                                               int64_t nb, int64_t d) {
-    int64_t lo = d > nb ? d - nb : 0, hi = d < na ? d : na;
-    while (lo < hi) {
-        const int64_t mid = (lo + hi) >> 1;
-        if (a[mid] < b[d - 1 - mid]) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
-}
-
-// One CTA per long bucket: sort SMALL_SEG chunks in shared memory, then merge
-// runs pairwise in global memory (keys <-> scratch), then write the result.
-__global__ void __launch_bounds__(BIG_THREADS) bucket_sort_big_kernel(
-    int32_t n_tiles, int64_t n_buckets, uint32_t tile_bits, const int32_t *__restrict__ offsets,
-    int64_t T, uint64_t *keys, uint64_t *scratch, int64_t *__restrict__ isect_ids,
-    int32_t *__restrict__ flatten_ids, const int32_t *big_list, const IsectHeader *hdr) {
-    __shared__ uint64_t s[SMALL_SEG];
-    const int n_big = hdr->n_big;
-    for (int item = blockIdx.x; item < n_big; item += gridDim.x) {
-    __syncthreads();
-    const int64_t bkt = big_list[item];
-    const int64_t lo = offsets[bkt];
-    const int64_t hi = (bkt + 1 < n_buckets) ? (int64_t)offsets[bkt + 1] : T;
-    const int64_t n = hi - lo;
-    uint64_t *src = keys + lo, *dst = scratch + lo;
-    for (int64_t c0 = 0; c0 < n; c0 += SMALL_SEG) {
-        const int cn = (int)imin64(SMALL_SEG, n - c0);
-        for (int i = threadIdx.x; i < SMALL_SEG; i += blockDim.x) s[i] = i < cn ? src[c0 + i] : ~0ull;
-        __syncthreads();
-        block_bitonic(s, SMALL_SEG);
-        for (int i = threadIdx.x; i < cn; i += blockDim.x) src[c0 + i] = s[i];
-        __syncthreads();
-    }
-    for (int64_t width = SMALL_SEG; width < n; width <<= 1) {
-        for (int64_t r0 = 0; r0 < n; r0 += 2 * width) {
-            const int64_t na = imin64(width, n - r0);
-            const int64_t nb = imin64(width, n - r0 - na);
-            const uint64_t *A = src + r0, *Bv = src + r0 + na;
-            uint64_t *O = dst + r0;
-            const int64_t total = na + nb;
-            for (int64_t o0 = (int64_t)threadIdx.x * MERGE_ITEMS; o0 < total;
-                 o0 += (int64_t)blockDim.x * MERGE_ITEMS) {
-                int64_t ia = merge_split(A, na, Bv, nb, o0);
-                int64_t ib = o0 - ia;
-                const int64_t oend = imin64(total, o0 + MERGE_ITEMS);
-                for (int64_t o = o0; o < oend; ++o) {
-                    const bool take_a = ib >= nb || (ia < na && A[ia] < Bv[ib]);
-                    O[o] = take_a ? A[ia++] : Bv[ib++];
-                }
-            }
-        }
-        __syncthreads();
-        uint64_t *t = src;
-        src = dst;
-        dst = t;
-    }
-    const int64_t cam = bkt / n_tiles, tile = bkt - cam * n_tiles;
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
-        write_sorted(src[i], lo + i, cam, tile, tile_bits, isect_ids, flatten_ids);
-    }
-}
+};
 
 // ---------------------------------------------------------- offset encode
 // offsets[b] = first sorted index whose (camera, tile) field is >= b: a
@@ -538,29 +317,16 @@ int ubs_isect_emit(int32_t C, int64_t N, const float *means2d, const int32_t *ra
         return check_launch("isect_emit_ordered");
     }
     if (cudaMemcpyAsync(w.cursor, isect_offsets, nb * 4, cudaMemcpyDeviceToDevice, st) !=
-            cudaSuccess ||
-        cudaMemsetAsync(&w.cw.hdr->n_big, 0, 4, st) != cudaSuccess)
+        cudaSuccess)
         return check_launch("isect_emit init");
     isect_emit_bucket_kernel<<<grid_for(CN, 256), 256, 0, st>>>(
         CN, N, m2, radii, depths, ts, (uint32_t)tile_width, (uint32_t)tile_height, w.cursor,
         w.keys, n_isects, &w.cw.hdr->status);
     ::ubs::note_launch();
-    bucket_sort_small_kernel<<<(unsigned)nb, SORT_THREADS, 0, st>>>(
-        nb, (int32_t)n_tiles, tile_bits, isect_offsets, n_isects, w.keys, isect_ids, flatten_ids,
-        w.big_list, w.cw.hdr);
-    ::ubs::note_launch();
-    if (int e = check_launch("isect bucket sort")) return e;
-    // long buckets (their number is only known on the device): a fixed grid
-    // walks the device-side list, so the host never waits here
-    if (n_isects > SMALL_SEG) {
-        const int64_t max_big = n_isects / (SMALL_SEG + 1);
-        const unsigned grid = (unsigned)imin64(imin64(max_big, nb), 304);
-        bucket_sort_big_kernel<<<grid, BIG_THREADS, 0, st>>>(
-            (int32_t)n_tiles, nb, tile_bits, isect_offsets, n_isects, w.keys, w.scratch,
-            isect_ids, flatten_ids, w.big_list, w.cw.hdr);
-    ::ubs::note_launch();
-    }
-    return check_launch("isect big-bucket sort");
+    if (int e = check_launch("isect emit")) return e;
+    const IdsWriter wr{isect_ids, flatten_ids, (int32_t)n_tiles, tile_bits};
+    return launch_bucket_sort(nb, isect_offsets, nullptr, n_isects, w.keys, w.scratch, w.big_list,
+                              &w.cw.hdr->n_big, wr, st);
 }
 
 int ubs_isect_offset_encode(int64_t n_isects, const int64_t *isect_ids, int32_t C,

@@ -55,7 +55,53 @@ struct RasterArgs {
     float *v_m2, *v_cn, *v_col, *v_op, *v_be;
     uint32_t *status;
     unsigned long long *pair_count; // contributing (pixel, record) pairs, or nullptr
+    // multi-view grids (nullptr: C views of W x H with the same TW x TH grid)
+    const int32_t *v_tile_base; // [C+1] first (view, tile) bucket of each view
+    const int32_t *v_dims;      // [C, 4] width, height, tile columns, tile rows
+    const int64_t *v_pix_base;  // [C] first pixel of each view in the image buffer
+    int32_t n_buckets;          // total (view, tile) buckets
+    const int64_t *n_isects_dev; // device-side intersection count (nullptr: n_isects)
 };
+
+// Where a (view, tile) bucket lives: view, tile within the view, image size,
+// tile columns and the view's first pixel.
+struct TileLoc {
+    int cam, tile, W, H, TW;
+    int64_t pix_base;
+};
+__device__ __forceinline__ TileLoc locate_tile(const RasterArgs &a, int bt) {
+    TileLoc l;
+    if (a.v_tile_base == nullptr) {
+        l.cam = bt / a.n_tiles;
+        l.tile = bt - l.cam * a.n_tiles;
+        l.W = a.W;
+        l.H = a.H;
+        l.TW = a.TW;
+        l.pix_base = (int64_t)l.cam * a.H * a.W;
+        return l;
+    }
+    int lo = 0, hi = a.C - 1; // last view whose first bucket is <= bt
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (a.v_tile_base[mid] <= bt) lo = mid;
+        else hi = mid - 1;
+    }
+    l.cam = lo;
+    l.tile = bt - a.v_tile_base[lo];
+    l.W = a.v_dims[lo * 4];
+    l.H = a.v_dims[lo * 4 + 1];
+    l.TW = a.v_dims[lo * 4 + 2];
+    l.pix_base = a.v_pix_base[lo];
+    return l;
+}
+
+// Number of valid sorted records: the device count (clamped to the record
+// capacity n_isects) when the counts never left the device.
+__device__ __forceinline__ int32_t isect_total(const RasterArgs &a) {
+    int64_t T = a.n_isects;
+    if (a.n_isects_dev) T = min(T, *a.n_isects_dev);
+    return (int32_t)T;
+}
 
 // ---------------------------------------------------------------- packing
 template <int CD, bool PACK>
@@ -230,16 +276,16 @@ __global__ void __launch_bounds__(512) raster_fwd_kernel(RasterArgs a) {
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int bt = blockIdx.x;
-    const int cam = bt / a.n_tiles;
-    const int tile = bt - cam * a.n_tiles;
-    const int ty = tile / a.TW, tx = tile - ty * a.TW;
+    const TileLoc loc = locate_tile(a, bt);
+    const int cam = loc.cam;
+    const int ty = loc.tile / loc.TW, tx = loc.tile - ty * loc.TW;
     const int wpr = a.TS >> 3;
     const int j = tx * a.TS + (warp % wpr) * 8 + (lane & 7);
     const int i0 = ty * a.TS + (warp / wpr) * 8 + (lane >> 3) * 2;
-    const bool in0 = (i0 < a.H) && (j < a.W);
-    const bool in1 = (i0 + 1 < a.H) && (j < a.W);
-    const int64_t pix0 = ((int64_t)cam * a.H + i0) * a.W + j;
-    const int64_t pix1 = pix0 + a.W;
+    const bool in0 = (i0 < loc.H) && (j < loc.W);
+    const bool in1 = (i0 + 1 < loc.H) && (j < loc.W);
+    const int64_t pix0 = loc.pix_base + (int64_t)i0 * loc.W + j;
+    const int64_t pix1 = pix0 + loc.W;
     const float *bg = a.bg ? a.bg + (int64_t)cam * CD : nullptr;
 
     if (a.masks && !a.masks[bt]) {
@@ -253,10 +299,11 @@ __global__ void __launch_bounds__(512) raster_fwd_kernel(RasterArgs a) {
         return;
     }
 
+    const int32_t T_all = isect_total(a);
     int32_t rs = a.offsets[bt];
-    int32_t re = (bt == a.C * a.n_tiles - 1) ? (int32_t)a.n_isects : a.offsets[bt + 1];
-    rs = max(0, min(rs, (int32_t)a.n_isects));
-    re = max(rs, min(re, (int32_t)a.n_isects));
+    int32_t re = (bt == a.n_buckets - 1) ? T_all : a.offsets[bt + 1];
+    rs = max(0, min(rs, T_all));
+    re = max(rs, min(re, T_all));
     const int nb = (re - rs + BR - 1) / BR;
 
     const float px = (float)j + 0.5f, py0 = (float)i0 + 0.5f, py1 = py0 + 1.f;
@@ -464,25 +511,25 @@ __global__ void __launch_bounds__(512) raster_bwd_kernel(RasterArgs a) {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int bt = blockIdx.x;
     if (a.masks && !a.masks[bt]) return;
-    const int cam = bt / a.n_tiles;
-    const int tile = bt - cam * a.n_tiles;
-    const int ty = tile / a.TW, tx = tile - ty * a.TW;
+    const TileLoc loc = locate_tile(a, bt);
+    const int cam = loc.cam;
+    const int ty = loc.tile / loc.TW, tx = loc.tile - ty * loc.TW;
     const int wpr = a.TS >> 3;
     const int j = tx * a.TS + (warp % wpr) * 8 + (lane & 7);
     const int i0 = ty * a.TS + (warp / wpr) * 8 + (lane >> 3) * 2;
-    const bool in0 = (i0 < a.H) && (j < a.W);
-    const bool in1 = (i0 + 1 < a.H) && (j < a.W);
+    const bool in0 = (i0 < loc.H) && (j < loc.W);
+    const bool in1 = (i0 + 1 < loc.H) && (j < loc.W);
     // outside pixels read a clamped pixel, like the reference, and never contribute
-    const int64_t img = (int64_t)a.W * a.H;
-    const int64_t base = (int64_t)cam * img;
-    const int64_t pix0 = base + min((int64_t)i0 * a.W + j, img - 1);
-    const int64_t pix1 = base + min((int64_t)(i0 + 1) * a.W + j, img - 1);
+    const int64_t img = (int64_t)loc.W * loc.H;
+    const int64_t pix0 = loc.pix_base + min((int64_t)i0 * loc.W + j, img - 1);
+    const int64_t pix1 = loc.pix_base + min((int64_t)(i0 + 1) * loc.W + j, img - 1);
     const float *bg = a.bg ? a.bg + (int64_t)cam * CD : nullptr;
 
+    const int32_t T_all = isect_total(a);
     int32_t rs = a.offsets[bt];
-    int32_t re = (bt == a.C * a.n_tiles - 1) ? (int32_t)a.n_isects : a.offsets[bt + 1];
-    rs = max(0, min(rs, (int32_t)a.n_isects));
-    re = max(rs, min(re, (int32_t)a.n_isects));
+    int32_t re = (bt == a.n_buckets - 1) ? T_all : a.offsets[bt + 1];
+    rs = max(0, min(rs, T_all));
+    re = max(rs, min(re, T_all));
 
     const float px = (float)j + 0.5f, py0 = (float)i0 + 0.5f, py1 = py0 + 1.f;
     BwdPix<CD> s0, s1;
@@ -633,7 +680,7 @@ static int launch_blend(RasterArgs &a, cudaStream_t st) {
     if (L.total > 227 * 1024)
         return set_error(UBS_ERR_UNSUPPORTED, "raster: tile_size %d with %d channels needs %d B "
                                               "of shared memory", a.TS, CD, L.total);
-    const unsigned nblocks = (unsigned)((int64_t)a.C * a.n_tiles);
+    const unsigned nblocks = (unsigned)a.n_buckets;
     if (nblocks == 0) return UBS_OK;
     auto k = BWD ? raster_bwd_kernel<CD, PACK> : raster_fwd_kernel<CD, PACK>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total) !=
@@ -717,6 +764,53 @@ static void fill_common(RasterArgs &a, int32_t C, int64_t N, int32_t ch, int64_t
     a.bg = bg;
     a.masks = masks;
     a.pair_count = nullptr;
+    a.v_tile_base = nullptr;
+    a.v_dims = nullptr;
+    a.v_pix_base = nullptr;
+    a.n_buckets = C * tw * th;
+    a.n_isects_dev = nullptr;
+}
+
+// Blend of the fused multi-view path (scene.cu): 3 colour channels packed
+// with the records, per-view grids, intersection count read on the device.
+int scene_blend(int fwd, int32_t C, int64_t CN, int32_t n_buckets, int32_t tile_size,
+                const int32_t *offsets, const int64_t *T_dev, int64_t cap, const void *recs,
+                const float4 *rcols, const float *bg, const int32_t *tile_base,
+                const int32_t *dims, const int64_t *pix_base, float *out_c, float *out_a,
+                int32_t *last_ids, const float *render_alphas, const int32_t *last_in,
+                const float *v_out_c, const float *v_out_a, float *v_m2, float *v_cn,
+                float *v_col, float *v_op, float *v_be, uint32_t *status, cudaStream_t st) {
+    RasterArgs a{};
+    a.C = C;
+    a.TS = tile_size;
+    a.n_isects = cap;
+    a.n_prims = CN;
+    a.offsets = offsets;
+    a.recs = static_cast<const GeoRec *>(recs);
+    a.rcols = rcols;
+    a.bg = bg;
+    a.status = status;
+    a.v_tile_base = tile_base;
+    a.v_dims = dims;
+    a.v_pix_base = pix_base;
+    a.n_buckets = n_buckets;
+    a.n_isects_dev = T_dev;
+    if (fwd) {
+        a.out_c = out_c;
+        a.out_a = out_a;
+        a.last_ids = last_ids;
+        return launch_blend<3, false>(a, st);
+    }
+    a.render_alphas = render_alphas;
+    a.last_in = last_in;
+    a.v_out_c = v_out_c;
+    a.v_out_a = v_out_a;
+    a.v_m2 = v_m2;
+    a.v_cn = v_cn;
+    a.v_col = v_col;
+    a.v_op = v_op;
+    a.v_be = v_be;
+    return launch_blend<3, true>(a, st);
 }
 
 } // namespace ubs

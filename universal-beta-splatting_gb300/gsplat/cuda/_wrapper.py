@@ -20,7 +20,8 @@ from ubs import _lib as L
 
 # Conditioning backward: "reference" reproduces the reference CUDA backward
 # (cond_mean_convariance_opacity_bwd.cu), including its transposed Cholesky
-# factor; "exact" returns the true gradient of the forward.
+# factor; "exact" returns the true gradient of the forward.  The mode in effect
+# when the forward runs is the one its backward uses.
 _COND_GRAD_MODE = os.environ.get("UBS_COND_GRAD", "reference")
 
 # channel counts with a dedicated kernel; others are padded (as the reference
@@ -73,6 +74,7 @@ class _CondMeanConvarianceOpacity(torch.autograd.Function):
         L.call("ubs_cond_fwd", N, D, L.ptr(means), L.ptr(covars), L.ptr(opacities), L.ptr(betas),
                L.ptr(query), L.ptr(om), L.ptr(oV), L.ptr(oo), L.stream(means.device))
         ctx.save_for_backward(means, covars, opacities, betas, query)
+        ctx.exact = _COND_GRAD_MODE == "exact"  # the mode at forward time applies
         return om, oV, oo
 
     @staticmethod
@@ -89,7 +91,7 @@ class _CondMeanConvarianceOpacity(torch.autograd.Function):
         gb = torch.empty(N, D - 3, device=dev)
         L.call("ubs_cond_bwd", N, D, L.ptr(means), L.ptr(covars), L.ptr(opacities), L.ptr(betas),
                L.ptr(query), L.ptr(v_m), L.ptr(v_V), L.ptr(v_o), L.ptr(gm), L.ptr(gV), L.ptr(go),
-               L.ptr(gb), 1 if _COND_GRAD_MODE == "exact" else 0, L.stream(dev))
+               L.ptr(gb), 1 if ctx.exact else 0, L.stream(dev))
         return gm, gV, go.view_as(opacities), gb, None
 
 

@@ -55,6 +55,12 @@ SIGNATURES = {
                               + [_P] * 2 + [_P] * 5 + [_I32, _P, _SZ, _P], _INT),
     "ubs_raster_status": ([_P, _U32P, ctypes.POINTER(ctypes.c_uint64), _P], _INT),
     "ubs_launch_count": ([], ctypes.c_ulonglong),
+    "ubs_scene_workspace_bytes": ([_I32, _I64, _I32, _I64], _SZ),
+    "ubs_scene_forward": ([_I32, _I64] + [_P] * 7 + [_I32] + [_P] * 7 + [_I32, _I32, _F, _F, _F, _F]
+                          + [_P] * 4 + [_I64, _P, _SZ, _P], _INT),
+    "ubs_scene_backward": ([_I32, _I64] + [_P] * 7 + [_I32] + [_P] * 7 + [_I32, _I32, _F, _F, _F, _F]
+                           + [_P] * 5 + [_P] * 7 + [_I32, _I64, _P, _SZ, _P], _INT),
+    "ubs_scene_stats": ([_P, _I64P, _U32P, _P], _INT),
     "ubs_fp32_probe_workspace_bytes": ([], _SZ),
     "ubs_fp32_probe": ([_I32, _P, _SZ, ctypes.POINTER(ctypes.c_double), _P], _INT),
 }

@@ -1,0 +1,211 @@
+"""Fused multi-view rendering of a Universal Beta Splatting scene (GB300 path).
+
+One call renders a batch of views, of any mix of resolutions and timestamps,
+with five stream-ordered launches (per-primitive forward, scan, emit, bucket
+sort, blend) and one autograd node whose backward is two launches (blend
+backward, per-primitive backward).  The mathematics is the reference model's
+render (scene/beta_model.py:660-722 + rendering.py:17-232), evaluated per
+(view, primitive): each primitive is conditioned on the ray to that view's
+camera (and its timestamp), so views are consistent with rendering them one at
+a time.
+
+    from ubs.render import Renderer, Views
+    r = Renderer(dim=6)
+    views = Views([cam0, cam1], device="cuda")      # ubs.scene.Camera objects
+    colors, alphas = r.render(params, views)       # flat [P, 3], [P]
+    images = views.split(colors)                   # list of [H, W, 3]
+"""
+import ctypes
+from typing import Dict, List, Optional, Sequence
+
+import torch
+
+from . import _lib as L
+
+PARAM_ORDER = ("xyz", "mean", "scale", "l_triangle", "opacity", "beta", "rgb")
+STATUS_OVERFLOW = 4
+STATUS_NEG_DEPTH = 2
+
+
+class Views:
+    """Cameras of one render call, flattened into (view, tile) buckets and one
+    pixel buffer.  `cameras` are ubs.scene.Camera objects (viewmat, K, width,
+    height, timestamp)."""
+
+    def __init__(self, cameras: Sequence, tile_size: int = 16, device=None):
+        if len(cameras) == 0:
+            raise ValueError("need at least one view")
+        device = torch.device(device or cameras[0].viewmat.device)
+        C = len(cameras)
+        vm = torch.stack([c.viewmat.reshape(16).float().cpu() for c in cameras])
+        intr = torch.tensor([[float(c.K[0, 0]), float(c.K[1, 1]), float(c.K[0, 2]),
+                              float(c.K[1, 2])] for c in cameras], dtype=torch.float32)
+        centers = torch.stack([c.center.float().cpu() for c in cameras])
+        times = torch.tensor([float(c.timestamp) for c in cameras], dtype=torch.float32)
+        dims, tile_base, pix_base = [], [0], [0]
+        for c in cameras:
+            tw = (c.width + tile_size - 1) // tile_size
+            th = (c.height + tile_size - 1) // tile_size
+            dims.append([c.width, c.height, tw, th])
+            tile_base.append(tile_base[-1] + tw * th)
+            pix_base.append(pix_base[-1] + c.width * c.height)
+        if tile_base[-1] >= 2 ** 31:
+            raise ValueError("too many tiles in one render call")
+        self.C = C
+        self.tile_size = tile_size
+        self.shapes = [(c.height, c.width) for c in cameras]
+        self.n_buckets = tile_base[-1]
+        self.n_pixels = pix_base[-1]
+        self.pix_base_host = pix_base
+        self.device = device
+        self.viewmats = vm.to(device)
+        self.intr = intr.to(device)
+        self.centers = centers.to(device)
+        self.times = times.to(device)
+        self.dims = torch.tensor(dims, dtype=torch.int32).to(device)
+        self.tile_base = torch.tensor(tile_base, dtype=torch.int32).to(device)
+        self.pix_base = torch.tensor(pix_base, dtype=torch.int64).to(device)
+
+    def split(self, flat: torch.Tensor) -> List[torch.Tensor]:
+        """Per-view [H, W, ...] views of a flat per-pixel buffer."""
+        out = []
+        for v, (h, w) in enumerate(self.shapes):
+            a, b = self.pix_base_host[v], self.pix_base_host[v + 1]
+            out.append(flat[a:b].view(h, w, *flat.shape[1:]))
+        return out
+
+    def join(self, images: Sequence[torch.Tensor]) -> torch.Tensor:
+        """Inverse of split: per-view [H, W, ...] tensors -> flat [P, ...]."""
+        return torch.cat([im.reshape(-1, *im.shape[2:]) for im in images], 0)
+
+
+class Renderer:
+    """Renders scenes through the fused path and keeps the intersection
+    capacity of its workspaces.  `exact_cond_grad` selects the exact
+    conditioning gradient instead of the reference's backward formula."""
+
+    def __init__(self, dim: int = 6, tile_size: int = 16, eps2d: float = 0.3,
+                 near_plane: float = 0.01, far_plane: float = 1e10, radius_clip: float = 0.0,
+                 capacity: Optional[int] = None, exact_cond_grad: bool = False):
+        if dim not in (6, 7):
+            raise ValueError("dim must be 6 or 7")
+        self.dim = dim
+        self.tile_size = tile_size
+        self.eps2d, self.near, self.far, self.radius_clip = eps2d, near_plane, far_plane, radius_clip
+        self.capacity = capacity
+        self.exact_cond_grad = exact_cond_grad
+        self.last_isects = None
+        self._pending = None  # (pinned stats, event, capacity) of an unchecked frame
+
+    # ---------------------------------------------------------------- helpers
+    def _check_pending(self):
+        if self._pending is None:
+            return
+        stats, ev, cap = self._pending
+        self._pending = None
+        ev.synchronize()
+        T, status = int(stats[0]), int(stats[1])
+        self.last_isects = T
+        if status & STATUS_NEG_DEPTH:
+            raise RuntimeError("scene render: a visible primitive has a negative depth")
+        if status & STATUS_OVERFLOW or T > cap:
+            self.capacity = max(self.capacity or 0, int(T * 1.25) + 1024)
+            raise RuntimeError("scene render: an earlier unchecked frame needed %d intersections "
+                               "but had capacity %d; capacity is now %d" % (T, cap, self.capacity))
+
+    def workspace_bytes(self, C, N, n_buckets, capacity):
+        return L.query("ubs_scene_workspace_bytes", C, N, n_buckets, capacity)
+
+    def _args(self, p, views, bg):
+        return [self.dim, p["xyz"].shape[0]] + [L.ptr(p[k]) for k in PARAM_ORDER] + [
+            views.C, L.ptr(views.viewmats), L.ptr(views.intr), L.ptr(views.centers),
+            L.ptr(views.times), L.ptr(views.dims), L.ptr(views.tile_base), L.ptr(views.pix_base),
+            views.n_buckets, self.tile_size, float(self.eps2d), float(self.near), float(self.far),
+            float(self.radius_clip), L.ptr(bg)]
+
+    def forward_raw(self, p: Dict[str, torch.Tensor], views: Views, bg, check=True):
+        """Run the forward kernels; returns (colors, alphas, last_ids, workspace, capacity)."""
+        self._check_pending()
+        N = p["xyz"].shape[0]
+        dev = p["xyz"].device
+        cap = self.capacity or max(1 << 16, 16 * N * views.C)
+        while True:
+            ws = L.workspace(self.workspace_bytes(views.C, N, views.n_buckets, cap), dev)
+            colors = torch.empty(views.n_pixels, 3, device=dev)
+            alphas = torch.empty(views.n_pixels, device=dev)
+            last = torch.empty(views.n_pixels, dtype=torch.int32, device=dev)
+            st = L.stream(dev)
+            L.call("ubs_scene_forward", *self._args(p, views, bg), L.ptr(colors), L.ptr(alphas),
+                   L.ptr(last), cap, L.ptr(ws), ws.numel(), st)
+            stats = torch.empty(2, dtype=torch.int64, pin_memory=True)
+            hdr = ws[:16].view(torch.int64)
+            if check:
+                stats.copy_(hdr.cpu())
+                T, status = int(stats[0]), int(stats[1]) & 0xffffffff
+                self.last_isects = T
+                if status & STATUS_NEG_DEPTH:
+                    raise RuntimeError("scene render: a visible primitive has a negative depth")
+                if T > cap:
+                    cap = int(T * 1.25) + 1024
+                    self.capacity = cap
+                    continue
+                if self.capacity is None:
+                    self.capacity = max(int(T * 1.25) + 1024, 1 << 16)
+            else:
+                stats.copy_(hdr, non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record()
+                self._pending = (stats, ev, cap)
+            return colors, alphas, last, ws, cap
+
+    def render(self, params: Dict[str, torch.Tensor], views: Views,
+               backgrounds: Optional[torch.Tensor] = None, check: bool = True):
+        """Differentiable render of all views: colors [P, 3], alphas [P]."""
+        dev = params["xyz"].device
+        if backgrounds is None:
+            bg = torch.zeros(views.C, 3, device=dev)
+        else:
+            bg = backgrounds.reshape(-1, 3).expand(views.C, 3).contiguous().float()
+        tensors = [params[k] for k in PARAM_ORDER]
+        return _SceneRender.apply(self, views, bg, check, *tensors)
+
+
+def _prep(t, shape_tail=None):
+    t = t.contiguous()
+    if t.dtype != torch.float32:
+        raise TypeError("scene parameters must be float32")
+    return t
+
+
+class _SceneRender(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, renderer, views, bg, check, xyz, mean, scale, l_triangle, opacity, beta, rgb):
+        p = {"xyz": _prep(xyz), "mean": _prep(mean), "scale": _prep(scale),
+             "l_triangle": _prep(l_triangle), "opacity": _prep(opacity.reshape(-1)),
+             "beta": _prep(beta), "rgb": _prep(rgb)}
+        colors, alphas, last, ws, cap = renderer.forward_raw(p, views, bg, check=check)
+        ctx.renderer, ctx.views, ctx.ws, ctx.cap = renderer, views, ws, cap
+        ctx.opacity_shape = opacity.shape
+        ctx.save_for_backward(p["xyz"], p["mean"], p["scale"], p["l_triangle"], p["opacity"],
+                              p["beta"], p["rgb"], bg, alphas, last)
+        ctx.mark_non_differentiable(last)
+        return colors, alphas
+
+    @staticmethod
+    def backward(ctx, v_colors, v_alphas):
+        xyz, mean, scale, ltri, opac, beta, rgb, bg, alphas, last = ctx.saved_tensors
+        r, views = ctx.renderer, ctx.views
+        dev = xyz.device
+        p = {"xyz": xyz, "mean": mean, "scale": scale, "l_triangle": ltri, "opacity": opac,
+             "beta": beta, "rgb": rgb}
+        v_colors = (torch.zeros(views.n_pixels, 3, device=dev) if v_colors is None
+                    else v_colors.contiguous())
+        v_alphas = (torch.zeros(views.n_pixels, device=dev) if v_alphas is None
+                    else v_alphas.contiguous())
+        g = {k: torch.empty_like(p[k]) for k in PARAM_ORDER}
+        L.call("ubs_scene_backward", *r._args(p, views, bg), L.ptr(alphas), L.ptr(last),
+               L.ptr(v_colors), L.ptr(v_alphas), *[L.ptr(g[k]) for k in PARAM_ORDER],
+               int(bool(r.exact_cond_grad)), ctx.cap, L.ptr(ctx.ws), ctx.ws.numel(), L.stream(dev))
+        ctx.ws = None
+        return (None, None, None, None, g["xyz"], g["mean"], g["scale"], g["l_triangle"],
+                g["opacity"].view(ctx.opacity_shape), g["beta"], g["rgb"])
