@@ -212,6 +212,29 @@ int ubs_raster_bwd_packed(int32_t C, int64_t N, int32_t channels, int64_t n_isec
                           float *v_betas, int32_t zero_outputs, void *workspace,
                           size_t workspace_bytes, void *stream);
 
+/* Forward blend without a workspace (no counterpart in the reference).
+ * Same arguments, results and errors as ubs_raster_fwd minus the workspace,
+ * for callers that cannot allocate device memory where they render (a host
+ * callback or real-time thread that must stay out of the CUDA allocator, or an
+ * application whose memory pool is fixed).  It allocates nothing: the packed
+ * records go to a fixed scratch array in the library's static device memory,
+ * 256 B + 48 B x UBS_RASTER_NOALLOC_MAX_ISECTS (24 MiB), one per device.
+ *   - n_isects above UBS_RASTER_NOALLOC_MAX_ISECTS returns UBS_ERR_OVERFLOW.
+ *   - The first call on a device looks the scratch address up (set-up work);
+ *     make it before capturing a stream.
+ *   - Nothing has to start at zero: each call clears the scratch's status
+ *     header on `stream` itself.
+ *   - One scratch per device: calls on the same device must not overlap in
+ *     time (two streams, or unordered host threads, race on the records). */
+#define UBS_RASTER_NOALLOC_MAX_ISECTS 524288
+int ubs_raster_fwd_noalloc(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
+                           const float *means2d, const float *conics, const float *colors,
+                           const float *opacities, const float *betas, const float *backgrounds,
+                           const uint8_t *masks, int32_t width, int32_t height, int32_t tile_size,
+                           int32_t tile_width, int32_t tile_height, const int32_t *isect_offsets,
+                           const int32_t *flatten_ids, float *render_colors, float *render_alphas,
+                           int32_t *last_ids, void *stream);
+
 /* ------------------------------------------------------- fused multi-view ---
  * One render of a Universal Beta Splatting scene into C views at once (no
  * single reference counterpart: it fuses the reference model's render,

@@ -53,6 +53,8 @@ SIGNATURES = {
                               + [_I32, _P, _SZ, _P], _INT),
     "ubs_raster_bwd_packed": ([_I32, _I64, _I32, _I64] + [_P] * 3 + [_I32] * 5 + [_P] * 3
                               + [_P] * 2 + [_P] * 5 + [_I32, _P, _SZ, _P], _INT),
+    "ubs_raster_fwd_noalloc": ([_I32, _I64, _I32, _I64] + [_P] * 7 + [_I32] * 5 + [_P] * 5 + [_P],
+                               _INT),
     "ubs_raster_status": ([_P, _U32P, ctypes.POINTER(ctypes.c_uint64), _P], _INT),
     "ubs_launch_count": ([], ctypes.c_ulonglong),
     "ubs_scene_workspace_bytes": ([_I32, _I64, _I32, _I64], _SZ),
