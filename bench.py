@@ -5,11 +5,14 @@ Workload (the reference's plain GPU configuration): 1,000,000 6-D Beta
 primitives (xyz uniform in [-2,2]^3, spatial scales exp(N(-4,0.5)), angular
 scales ~1, rest lower-triangle N(0,0.1), angular raw betas N(0,0.5), spatial raw
 beta N(0,0.3), opacity logits N(0,1), RGB uniform), one 1920x1080 pinhole camera
-(fx=fy=1500) on a radius-4 orbit, 16x16 tiles.  One step = forward render through
-the reference's call sequence (activations, rotation, covariance, conditioning,
+(fx=fy=1500) on a radius-4 orbit, 16x16 tiles.  One step = forward render of the
+reference model's render (activations, rotation, covariance, conditioning,
 projection, intersection + sort, blend), an L1 loss against a random target and
-the backward pass to all raw parameters.  Data are seeded synthetic tensors with
-the benchmark's distributions (the reference's datasets are not available).
+the backward pass to all raw parameters.  The headline runs the fused scene
+render (ubs.render); the same step through the drop-in gsplat operators and
+through the reference's own CUDA kernels (plain one-view-per-launch form) is
+timed beside it.  Data are seeded synthetic tensors with the benchmark's
+distributions (the reference's datasets are not available).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -54,6 +57,9 @@ def parse():
     ap.add_argument("--n-prims", type=int, default=N_PRIMS)
     ap.add_argument("--no-ref-gpu", action="store_true", help="skip timing the reference kernels")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--profile", action="store_true",
+                    help="run only the fused step (first frame, --warmup steps, one more step) "
+                         "for an ncu capture; prints no JSON line")
     return ap.parse_args()
 
 
@@ -148,6 +154,36 @@ def gpu_step(p, cam, ri, rj, bg, target):
     loss = (img - target).abs().mean()
     loss.backward()
     return loss, meta
+
+
+class FusedStep:
+    """One training step through the fused scene render: forward of the view,
+    L1 loss against the target, backward to all raw parameters."""
+
+    def __init__(self, p, cam, bg, target, dev):
+        from ubs.render import Renderer, Views
+        self.p = p
+        self.renderer = Renderer(dim=DIM, tile_size=TILE)
+        self.views = Views([cam], tile_size=TILE, device=dev)
+        self.bg = bg.reshape(1, 3).contiguous()
+        self.target = target.permute(1, 2, 0).reshape(-1, 3).contiguous()
+
+    def prime(self):
+        """First frame with a synchronous capacity check (sizes the buffers)."""
+        with torch.no_grad():
+            self.renderer.render(self.p, self.views, self.bg, check=True)
+
+    def step(self):
+        for v in self.p.values():
+            v.grad = None
+        colors, _ = self.renderer.render(self.p, self.views, self.bg, check=False)
+        loss = (colors - self.target).abs().mean()
+        loss.backward()
+        return loss
+
+    def forward(self):
+        with torch.no_grad():
+            self.renderer.render(self.p, self.views, self.bg, check=False)
 
 
 def time_steps(fn, K, dev, flush):
@@ -359,12 +395,21 @@ def main():
     from ubs import _lib as L
     L.lib()
     p, cam, ri, rj, bg, target = make_problem(args.n_prims, rank, dev)
+    fz = FusedStep(p, cam, bg, target, dev)
+    if args.profile:
+        fz.prime()
+        for _ in range(args.warmup + 1):
+            fz.step()
+        torch.cuda.synchronize()
+        fz.renderer._check_pending()
+        print("profile run: %d intersections" % fz.renderer.last_isects, flush=True)
+        return
     flush = l2_flush_buffer(dev)
     clocks = ClockSampler()
     clocks.start()
-    step = lambda: gpu_step(p, cam, ri, rj, bg, target)  # noqa: E731
+    fz.prime()
     for _ in range(max(3, args.warmup)):
-        step()
+        fz.step()
     torch.cuda.synchronize()
     if world > 1:
         import torch.distributed as dist
@@ -373,10 +418,13 @@ def main():
     launches0 = L.query("ubs_launch_count")
     clocks.mark("t0")
     t_wall = time.perf_counter()
-    ms = time_steps(step, args.steps, dev, flush)
+    L.profile_start(64 * (args.steps + 1))
+    ms = time_steps(fz.step, args.steps, dev, flush)
+    kernels = L.profile_stop()
     wall = time.perf_counter() - t_wall
     clocks.mark("t1")
-    launches = (L.query("ubs_launch_count") - launches0) // max(1, args.steps)
+    fz.renderer._check_pending()  # raises if any timed frame overflowed its buffers
+    launches = L.query("ubs_launch_count") - launches0
     torch.cuda.synchronize()
     ms_max = ms
     if world > 1:
@@ -386,11 +434,12 @@ def main():
         ms_max = float(t.item())
         dist.barrier()
     value = world * 1000.0 / ms_max
+    kernel_ms = {k: t / args.steps for k, (n, t) in kernels.items()}
 
-    # end to end: parameters and target from pinned host memory every step,
-    # the loss read back
+    # end to end through the public API: parameters and target copied from
+    # pinned host memory every step, the loss read back
     host = {k: v.detach().cpu().pin_memory() for k, v in p.items()}
-    host_target = target.cpu().pin_memory()
+    host_target = fz.target.cpu().pin_memory()
     h2d = sum(v.numel() * 4 for v in host.values()) + host_target.numel() * 4
     loss_host = torch.empty(1, pin_memory=True)
 
@@ -398,22 +447,32 @@ def main():
         with torch.no_grad():
             for k, v in p.items():
                 v.copy_(host[k], non_blocking=True)
-            target.copy_(host_target, non_blocking=True)
-        loss, _ = gpu_step(p, cam, ri, rj, bg, target)
+            fz.target.copy_(host_target, non_blocking=True)
+        loss = fz.step()
         loss_host.copy_(loss.detach().view(1), non_blocking=True)
 
     for _ in range(2):
         e2e_step()
     e2e_ms = time_steps(e2e_step, args.steps, dev, flush)
+    fz.renderer._check_pending()
     e2e_val = world * 1000.0 / e2e_ms
     clocks.stop()
+    fwd_ms = time_steps(fz.forward, max(5, min(args.steps, 20)), dev, flush)
+    fz.renderer._check_pending()
 
-    # per-entry-point times (CUDA events on the launching stream)
+    # the drop-in operator sequence (gsplat.rendering.rasterization call path)
     K2 = max(5, min(args.steps, 20))
-    L.start_timing()
-    for _ in range(K2):
-        step()
-    stages = {k: t / K2 for k, (n, t) in L.stop_timing().items()}
+    d_step = lambda: gpu_step(p, cam, ri, rj, bg, target)  # noqa: E731
+    for _ in range(3):
+        d_step()
+    d_ms = time_steps(d_step, K2, dev, flush)
+
+    def d_fwd():
+        from ubs import scene as S
+        with torch.no_grad():
+            S.render_view(p, cam, bg, ri, rj, tile_size=TILE)
+    d_fwd_ms = time_steps(d_fwd, K2, dev, flush)
+
     pairs, n_isects, n_visible = count_pairs(p, cam, ri, rj, bg, dev)
     peak_fp32 = fp32_peak(dev)
     peaks = {}
@@ -421,19 +480,21 @@ def main():
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except (OSError, ValueError):
         pass
-    dominant = max(stages, key=stages.get)
-    dom_ms = stages[dominant]
-    flop_pp = BWD_FLOP_PER_PAIR if "bwd" in dominant else FWD_FLOP_PER_PAIR
+    dominant = max(kernel_ms, key=kernel_ms.get)
+    n_dom, t_dom = kernels[dominant]
+    dom_ms = t_dom / n_dom
+    flop_pp = BWD_FLOP_PER_PAIR if dominant == "raster_bwd" else FWD_FLOP_PER_PAIR
     achieved = pairs * flop_pp / (dom_ms * 1e-3) / 1e12
     roofline = {
         "kernel": dominant, "bound": "fp32",
         "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s",
         "frac": achieved / peak_fp32 if peak_fp32 else None,
         "traffic": read_profile_traffic(dominant),
-        "algorithmic_work": "%d contributing pairs x %d FP32 ops" % (pairs, flop_pp),
-        "peak_source": "FP32 FMA probe kernel timed in this run (MEASURED_PEAKS.json has HBM "
-                       "%s GB/s and bf16 only)" % peaks.get("hbm_gbs", "n/a"),
+        "algorithmic_work": "%d contributing pairs x %d FP32 ops per launch" % (pairs, flop_pp),
+        "peak_source": "measured: FP32 FMA probe kernel timed in this run (MEASURED_PEAKS.json "
+                       "has HBM %s GB/s and bf16 only)" % peaks.get("hbm_gbs", "n/a"),
         "launch_ms": dom_ms,
+        "timing": "CUDA events on the launching stream around each launch, timed region",
     }
 
     # the reference's own kernels, plain one-view-per-launch path, same GPU
@@ -451,13 +512,21 @@ def main():
                                                bg, ri, rj, tile_size=TILE)
                     (img - target).abs().mean().backward()
 
+                def ref_fwd():
+                    with torch.no_grad():
+                        rp.render_view(p, cam.viewmat, cam.K, WIDTH, HEIGHT, cam.center, bg, ri,
+                                       rj, tile_size=TILE)
+
                 for _ in range(3):
                     ref_step()
-                r_ms = time_steps(ref_step, max(5, min(args.steps, 20)), dev, flush)
+                r_ms = time_steps(ref_step, K2, dev, flush)
+                r_fwd_ms = time_steps(ref_fwd, K2, dev, flush)
                 ref_gpu = {"value": 1000.0 / r_ms, "unit": "it/s", "ms_per_step": r_ms,
+                           "render_fps": 1000.0 / r_fwd_ms,
                            "what": "the reference's CUDA kernels (built from its sources for "
-                                   "sm_103) in its plain call sequence on this GPU; intersections "
-                                   "sorted with torch.sort in place of its cub sort"}
+                                   "sm_103) in its plain one-view-per-launch call sequence on "
+                                   "this GPU; intersections sorted with torch.sort in place of "
+                                   "its cub sort"}
         except Exception as e:  # noqa: BLE001
             ref_gpu = {"error": str(e)[:200]}
 
@@ -468,13 +537,6 @@ def main():
             cpu = {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")}
         except Exception as e:  # noqa: BLE001
             cpu = {"error": str(e)[:200]}
-
-    # render-only frames/s (forward, no grad)
-    def fwd_only():
-        from ubs import scene as S
-        with torch.no_grad():
-            S.render_view(p, cam, bg, ri, rj, tile_size=TILE)
-    fwd_ms = time_steps(fwd_only, max(5, min(args.steps, 20)), dev, flush)
 
     if rank == 0:
         line = {
@@ -487,17 +549,21 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "256 MB buffer written before every timed step (untimed); "
                              "per-step CUDA events",
-                       "path": "drop-in operators (gsplat.rendering.rasterization call sequence)"},
+                       "path": "fused scene render (ubs.render.Renderer)"},
             "render_fps": 1000.0 / fwd_ms,
             "e2e": {"value": e2e_val, "unit": "it/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": 4},
-            "gpu_launches": int(launches) * args.steps,
-            "launches_per_step": int(launches),
+            "gpu_launches": int(launches),
+            "launches_per_step": int(launches) // max(1, args.steps),
             "roofline": roofline,
             "cpu_baseline": cpu,
             "ref_gpu": ref_gpu,
+            "dropin": {"value": 1000.0 / d_ms, "unit": "it/s", "ms_per_step": d_ms,
+                       "render_fps": 1000.0 / d_fwd_ms,
+                       "what": "the same step through the drop-in gsplat operators"},
             "clocks": clocks.summary(clocks.marks.get("t0", 0), clocks.marks.get("t1", 0)),
-            "stages_ms": {k: round(v, 4) for k, v in sorted(stages.items(), key=lambda x: -x[1])},
+            "kernels_ms_per_step": {k: round(v, 4) for k, v in
+                                    sorted(kernel_ms.items(), key=lambda x: -x[1])},
             "isects": n_isects, "visible": n_visible, "pairs": pairs,
             "wall_s_timed": wall,
         }

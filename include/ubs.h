@@ -42,6 +42,16 @@ int ubs_abi_version(void);
 /* Number of kernels this library has launched in the process (no reference
  * counterpart; used to report launches per benchmark step). */
 unsigned long long ubs_launch_count(void);
+/* Kernel timing (no reference counterpart).  Between ubs_profile_start and
+ * ubs_profile_stop every kernel the library launches (from any thread) is
+ * bracketed by a pair of CUDA events recorded on its launching stream, from a
+ * pool of max_launches pairs created by start (launches beyond the pool are
+ * not timed).  stop waits for the recorded events and aggregates the
+ * durations per kernel name; ubs_profile_result(i, ...) reads entry i < n.
+ * Start and stop are host-side set-up: call them outside stream capture. */
+int ubs_profile_start(int32_t max_launches);
+int ubs_profile_stop(int32_t *n_kernels);
+int ubs_profile_result(int32_t i, const char **name, int64_t *launches, double *total_ms);
 /* FP32 FMA issue-rate probe (no reference counterpart): 8 CTAs of 256 threads
  * per SM run independent FMA chains; *flops receives the launch's FP32 operation
  * count so that the caller's event timing gives the measured FP32 peak used as

@@ -1,7 +1,11 @@
 // core.cu -- error state and version of the C ABI.
+#include <algorithm>
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
 
 #include "ubs_common.cuh"
 
@@ -42,6 +46,45 @@ int check_launch(const char *what) {
     return set_error(UBS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
+// ------------------------------------------------------------ kernel timing
+namespace {
+struct ProfSlot {
+    const char *name;
+    cudaEvent_t e0, e1;
+};
+struct ProfEntry {
+    const char *name;
+    long long launches;
+    double ms;
+};
+std::mutex g_prof_mu;
+std::vector<ProfSlot> g_prof_slots;
+std::vector<ProfEntry> g_prof_result;
+std::atomic<bool> g_prof_on{false};
+std::atomic<int> g_prof_next{0};
+} // namespace
+
+KernelTimer::KernelTimer(const char *name, cudaStream_t s) : slot(-1), st(s) {
+    if (!g_prof_on.load(std::memory_order_acquire)) return;
+    const int i = g_prof_next.fetch_add(1, std::memory_order_relaxed);
+    if (i >= (int)g_prof_slots.size()) return; // pool exhausted: launch is not timed
+    g_prof_slots[i].name = name;
+    if (cudaEventRecord(g_prof_slots[i].e0, st) == cudaSuccess) slot = i;
+}
+
+KernelTimer::~KernelTimer() {
+    if (slot >= 0 && cudaEventRecord(g_prof_slots[slot].e1, st) != cudaSuccess)
+        g_prof_slots[slot].name = nullptr;
+}
+
+static void prof_release() {
+    for (auto &p : g_prof_slots) {
+        cudaEventDestroy(p.e0);
+        cudaEventDestroy(p.e1);
+    }
+    g_prof_slots.clear();
+}
+
 } // namespace ubs
 
 extern "C" {
@@ -74,6 +117,68 @@ int ubs_fp32_probe(int32_t iters, void *workspace, size_t workspace_bytes, doubl
     ubs::note_launch();
     if (flops) *flops = 2.0 * 8 * 16 * (double)iters * sms * 8 * 256;
     return ubs::check_launch("fp32_probe");
+}
+
+int ubs_profile_start(int32_t max_launches) {
+    using namespace ubs;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    if (g_prof_on.load()) return set_error(UBS_ERR_INVALID, "profile_start: already running");
+    if (max_launches < 1 || max_launches > (1 << 20))
+        return set_error(UBS_ERR_INVALID, "profile_start: max_launches %d not in [1, 2^20]",
+                         max_launches);
+    if ((int)g_prof_slots.size() != max_launches) {
+        prof_release();
+        g_prof_slots.resize(max_launches);
+        for (auto &p : g_prof_slots) {
+            p.name = nullptr;
+            if (cudaEventCreate(&p.e0) != cudaSuccess || cudaEventCreate(&p.e1) != cudaSuccess) {
+                g_prof_slots.clear();
+                return check_launch("profile_start event pool");
+            }
+        }
+    }
+    g_prof_result.clear();
+    g_prof_next.store(0);
+    g_prof_on.store(true, std::memory_order_release);
+    return UBS_OK;
+}
+
+int ubs_profile_stop(int32_t *n_kernels) {
+    using namespace ubs;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    if (!g_prof_on.load()) return set_error(UBS_ERR_INVALID, "profile_stop: not running");
+    g_prof_on.store(false, std::memory_order_release);
+    const int n = std::min<int>(g_prof_next.load(), (int)g_prof_slots.size());
+    for (int i = 0; i < n; ++i) {
+        const ProfSlot &p = g_prof_slots[i];
+        if (!p.name) continue;
+        float ms = 0.f;
+        if (cudaEventSynchronize(p.e1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, p.e0, p.e1) != cudaSuccess)
+            return check_launch("profile_stop");
+        ProfEntry *e = nullptr;
+        for (auto &r : g_prof_result)
+            if (std::strcmp(r.name, p.name) == 0) e = &r;
+        if (!e) {
+            g_prof_result.push_back({p.name, 0, 0.0});
+            e = &g_prof_result.back();
+        }
+        e->launches += 1;
+        e->ms += ms;
+    }
+    if (n_kernels) *n_kernels = (int32_t)g_prof_result.size();
+    return UBS_OK;
+}
+
+int ubs_profile_result(int32_t i, const char **name, int64_t *launches, double *total_ms) {
+    using namespace ubs;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    if (i < 0 || i >= (int)g_prof_result.size())
+        return set_error(UBS_ERR_INVALID, "profile_result: index %d out of range", i);
+    if (name) *name = g_prof_result[i].name;
+    if (launches) *launches = g_prof_result[i].launches;
+    if (total_ms) *total_ms = g_prof_result[i].ms;
+    return UBS_OK;
 }
 
 } // extern "C"

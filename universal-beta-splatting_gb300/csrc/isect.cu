@@ -260,10 +260,11 @@ int ubs_isect_count(int32_t C, int64_t N, const float *means2d, const int32_t *r
         cudaMemsetAsync(w.bucket_counts, 0, nb * 4, st) != cudaSuccess)
         return check_launch("isect_count memset");
     if (CN > 0)
-        isect_count_kernel<<<grid_for(CN, 256), 256, 0, st>>>(
-            CN, N, reinterpret_cast<const float2 *>(means2d), radii, depths, (float)tile_size,
-            (uint32_t)tile_width, (uint32_t)tile_height, tiles_per_gauss, w.bucket_counts,
-            &w.hdr->status);
+        UBS_TIMED("isect_count", st,
+                  isect_count_kernel<<<grid_for(CN, 256), 256, 0, st>>>(
+                      CN, N, reinterpret_cast<const float2 *>(means2d), radii, depths,
+                      (float)tile_size, (uint32_t)tile_width, (uint32_t)tile_height,
+                      tiles_per_gauss, w.bucket_counts, &w.hdr->status));
     ::ubs::note_launch();
     if (int e = check_launch("isect_count")) return e;
     if (int e = device_exclusive_scan<int32_t>(w.bucket_counts, isect_offsets, nb, w.block_sums,
@@ -310,18 +311,21 @@ int ubs_isect_emit(int32_t C, int64_t N, const float *means2d, const int32_t *ra
         if (int e = device_exclusive_scan<int64_t>(tiles_per_gauss, w.prim_start, CN,
                                                    w.cw.block_sums, tot, st))
             return e;
-        isect_emit_ordered_kernel<<<grid_for(CN, 256), 256, 0, st>>>(
-            CN, N, m2, radii, depths, ts, (uint32_t)tile_width, (uint32_t)tile_height, tile_bits,
-            w.prim_start, isect_ids, flatten_ids, n_isects, &w.cw.hdr->status);
+        UBS_TIMED("isect_emit_ordered", st,
+                  isect_emit_ordered_kernel<<<grid_for(CN, 256), 256, 0, st>>>(
+                      CN, N, m2, radii, depths, ts, (uint32_t)tile_width, (uint32_t)tile_height,
+                      tile_bits, w.prim_start, isect_ids, flatten_ids, n_isects,
+                      &w.cw.hdr->status));
     ::ubs::note_launch();
         return check_launch("isect_emit_ordered");
     }
     if (cudaMemcpyAsync(w.cursor, isect_offsets, nb * 4, cudaMemcpyDeviceToDevice, st) !=
         cudaSuccess)
         return check_launch("isect_emit init");
-    isect_emit_bucket_kernel<<<grid_for(CN, 256), 256, 0, st>>>(
-        CN, N, m2, radii, depths, ts, (uint32_t)tile_width, (uint32_t)tile_height, w.cursor,
-        w.keys, n_isects, &w.cw.hdr->status);
+    UBS_TIMED("isect_emit", st,
+              isect_emit_bucket_kernel<<<grid_for(CN, 256), 256, 0, st>>>(
+                  CN, N, m2, radii, depths, ts, (uint32_t)tile_width, (uint32_t)tile_height,
+                  w.cursor, w.keys, n_isects, &w.cw.hdr->status));
     ::ubs::note_launch();
     if (int e = check_launch("isect emit")) return e;
     const IdsWriter wr{isect_ids, flatten_ids, (int32_t)n_tiles, tile_bits};
@@ -342,8 +346,10 @@ int ubs_isect_offset_encode(int64_t n_isects, const int64_t *isect_ids, int32_t 
             return check_launch("offset_encode memset");
         return UBS_OK;
     }
-    offset_encode_kernel<<<grid_for(nb, 256), 256, 0, st>>>(
-        n_isects, isect_ids, nb, (int32_t)n_tiles, bit_width_u32((uint32_t)n_tiles), offsets);
+    UBS_TIMED("offset_encode", st,
+              offset_encode_kernel<<<grid_for(nb, 256), 256, 0, st>>>(
+                  n_isects, isect_ids, nb, (int32_t)n_tiles, bit_width_u32((uint32_t)n_tiles),
+                  offsets));
     ::ubs::note_launch();
     return check_launch("offset_encode");
 }

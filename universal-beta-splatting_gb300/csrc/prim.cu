@@ -426,8 +426,9 @@ int ubs_l_triangle_to_rotmat_fwd(int64_t n, const float *l_triangle, int64_t row
                                  float *rotmats, void *stream) {
     UBS_REQUIRE(n >= 0 && row_stride >= 3, "rotmat_fwd: bad sizes");
     if (n == 0) return UBS_OK;
-    rotmat_fwd_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(n, l_triangle,
-                                                                          row_stride, rotmats);
+    UBS_TIMED("rotmat_fwd", (cudaStream_t)stream,
+              rotmat_fwd_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(
+                  n, l_triangle, row_stride, rotmats));
     ::ubs::note_launch();
     return finish("rotmat_fwd");
 }
@@ -436,8 +437,9 @@ int ubs_l_triangle_to_rotmat_bwd(int64_t n, const float *v_rotmats, float *v_l_t
                                  void *stream) {
     UBS_REQUIRE(n >= 0, "rotmat_bwd: bad sizes");
     if (n == 0) return UBS_OK;
-    rotmat_bwd_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(n, v_rotmats,
-                                                                          v_l_triangle);
+    UBS_TIMED("rotmat_bwd", (cudaStream_t)stream,
+              rotmat_bwd_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(
+                  n, v_rotmats, v_l_triangle));
     ::ubs::note_launch();
     return finish("rotmat_bwd");
 }
@@ -466,9 +468,10 @@ int ubs_rot_scale_l_triangle_to_covar_fwd(int64_t n, int32_t dim, const float *r
                 m_rest);
     if (n == 0) return UBS_OK;
     cudaStream_t st = (cudaStream_t)stream;
-    UBS_DIM_SWITCH(dim, covar_fwd_kernel<DD><<<grid_for(n, 128), 128, 0, st>>>(
-                            n, rot, scale, l_triangle, rest_i, rest_j, m_rest, spatial_block,
-                            covar));
+    UBS_TIMED("covar_fwd", st,
+              UBS_DIM_SWITCH(dim, covar_fwd_kernel<DD><<<grid_for(n, 128), 128, 0, st>>>(
+                                      n, rot, scale, l_triangle, rest_i, rest_j, m_rest,
+                                      spatial_block, covar)));
     ::ubs::note_launch();
     return finish("covar_fwd");
 }
@@ -482,9 +485,10 @@ int ubs_rot_scale_l_triangle_to_covar_bwd(int64_t n, int32_t dim, const float *r
     UBS_REQUIRE(n >= 0 && m_rest >= 0 && m_rest <= 64, "covar_bwd: bad sizes");
     if (n == 0) return UBS_OK;
     cudaStream_t st = (cudaStream_t)stream;
-    UBS_DIM_SWITCH(dim, covar_bwd_kernel<DD><<<grid_for(n, 128), 128, 0, st>>>(
-                            n, rot, scale, l_triangle, rest_i, rest_j, m_rest, spatial_block,
-                            v_covar, v_rot, v_scale, v_l_triangle));
+    UBS_TIMED("covar_bwd", st,
+              UBS_DIM_SWITCH(dim, covar_bwd_kernel<DD><<<grid_for(n, 128), 128, 0, st>>>(
+                                      n, rot, scale, l_triangle, rest_i, rest_j, m_rest,
+                                      spatial_block, v_covar, v_rot, v_scale, v_l_triangle)));
     ::ubs::note_launch();
     return finish("covar_bwd");
 }
@@ -508,9 +512,10 @@ int ubs_cond_fwd(int64_t n, int32_t dim, const float *means, const float *covars
     UBS_REQUIRE(n >= 0 && dim >= 4, "cond_fwd: bad sizes (dim %d)", dim);
     if (n == 0) return UBS_OK;
     cudaStream_t st = (cudaStream_t)stream;
-    UBS_K_SWITCH(dim - 3, cond_fwd_kernel<KK><<<grid_for(n, 128), 128, 0, st>>>(
-                              n, means, covars, opacities, betas, query, out_means, out_covars,
-                              out_opacities));
+    UBS_TIMED("cond_fwd", st,
+              UBS_K_SWITCH(dim - 3, cond_fwd_kernel<KK><<<grid_for(n, 128), 128, 0, st>>>(
+                                        n, means, covars, opacities, betas, query, out_means,
+                                        out_covars, out_opacities)));
     ::ubs::note_launch();
     return finish("cond_fwd");
 }
@@ -523,10 +528,11 @@ int ubs_cond_bwd(int64_t n, int32_t dim, const float *means, const float *covars
     UBS_REQUIRE(n >= 0 && dim >= 4, "cond_bwd: bad sizes (dim %d)", dim);
     if (n == 0) return UBS_OK;
     cudaStream_t st = (cudaStream_t)stream;
-    UBS_K_SWITCH(dim - 3, cond_bwd_kernel<KK><<<grid_for(n, 128), 128, 0, st>>>(
-                              n, means, covars, opacities, betas, query, v_out_means,
-                              v_out_covars, v_out_opacities, v_means, v_covars, v_opacities,
-                              v_betas, exact));
+    UBS_TIMED("cond_bwd", st,
+              UBS_K_SWITCH(dim - 3, cond_bwd_kernel<KK><<<grid_for(n, 128), 128, 0, st>>>(
+                                        n, means, covars, opacities, betas, query, v_out_means,
+                                        v_out_covars, v_out_opacities, v_means, v_covars,
+                                        v_opacities, v_betas, exact)));
     ::ubs::note_launch();
     return finish("cond_bwd");
 }
@@ -573,7 +579,8 @@ int ubs_projection_fwd(int32_t C, int64_t N, const float *means, const float *co
     a.comps = compensations;
     const int64_t CN = (int64_t)C * N;
     if (CN == 0) return UBS_OK;
-    projection_fwd_kernel<<<grid_for(CN, 256), 256, 0, (cudaStream_t)stream>>>(a);
+    UBS_TIMED("projection_fwd", (cudaStream_t)stream,
+              projection_fwd_kernel<<<grid_for(CN, 256), 256, 0, (cudaStream_t)stream>>>(a));
     ::ubs::note_launch();
     return finish("projection_fwd");
 }
@@ -618,7 +625,7 @@ int ubs_projection_bwd(int32_t C, int64_t N, const float *means, const float *co
         return finish("projection_bwd memset");
     const int64_t CN = (int64_t)C * N;
     if (CN == 0) return UBS_OK;
-    projection_bwd_kernel<<<grid_for(CN, 256), 256, 0, st>>>(a);
+    UBS_TIMED("projection_bwd", st, projection_bwd_kernel<<<grid_for(CN, 256), 256, 0, st>>>(a));
     ::ubs::note_launch();
     return finish("projection_bwd");
 }

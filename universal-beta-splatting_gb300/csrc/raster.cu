@@ -166,17 +166,40 @@ __host__ __device__ inline SmemLayout smem_layout(int NT) {
     return L;
 }
 
-// Conservative pixel-centre bounding box of {d : d^T Q d < 1} for the conic
-// Q = [[cxx, cxy], [cxy, cyy]].  Returns false (no culling) for conics that are
-// not positive definite or so elongated that FP32 rounding of sigma could put a
-// pixel outside the exact ellipse below 1.
-__device__ __forceinline__ bool conic_box(const GeoRec &r, float &ex, float &ey) {
+// Whether the ellipse {d : d^T Q d < 1} of a record (Q its conic, d = centre -
+// pixel) can hold a pixel centre of the 8x8 box [bx0, bx0 + 7] x [by0, by0 + 7].
+// The quadratic is minimised over the box: it is zero when the centre lies in
+// the box; otherwise the minimum lies on an edge whose outside holds the
+// centre (for a convex function the segment from the box minimiser towards the
+// unconstrained minimiser leaves the box), so only the one or two facing edges
+// are searched, each in closed form.  The test is conservative: the pixel grid
+// is treated as continuous and the threshold has 1% slack for FP32 rounding of
+// sigma; conics that are not positive definite or are so elongated that
+// rounding could matter are never culled (pd == false).
+__device__ __forceinline__ bool conic_pd(const GeoRec &r) {
     const float det = r.cxx * r.cyy - r.cxy * r.cxy;
-    const bool ok = (r.cxx > 0.f) && (r.cyy > 0.f) && (det > 1e-3f * r.cxx * r.cyy);
-    if (!ok) return false;
-    ex = sqrtf(r.cyy / det) * 1.002f + 1e-2f;
-    ey = sqrtf(r.cxx / det) * 1.002f + 1e-2f;
-    return true;
+    return (r.cxx > 0.f) && (r.cyy > 0.f) && (det > 1e-3f * r.cxx * r.cyy);
+}
+__device__ __forceinline__ bool ellipse_hits_box(const GeoRec &r, bool pd, float bx0, float by0) {
+    if (!pd) return true;
+    const float ex = fminf(fmaxf(r.x, bx0), bx0 + 7.f); // nearest box point to the centre
+    const float ey = fminf(fmaxf(r.y, by0), by0 + 7.f);
+    const bool out_x = ex != r.x, out_y = ey != r.y;
+    if (!out_x && !out_y) return true;
+    float best = 3.0e38f;
+    if (out_x) { // edge x = ex: minimise over y in [by0, by0 + 7]
+        const float dx = r.x - ex;
+        const float y = fminf(fmaxf(r.y + r.cxy * dx / r.cyy, by0), by0 + 7.f);
+        const float dy = r.y - y;
+        best = r.cxx * dx * dx + 2.f * r.cxy * dx * dy + r.cyy * dy * dy;
+    }
+    if (out_y) { // edge y = ey: minimise over x in [bx0, bx0 + 7]
+        const float dy = r.y - ey;
+        const float x = fminf(fmaxf(r.x + r.cxy * dy / r.cxx, bx0), bx0 + 7.f);
+        const float dx = r.x - x;
+        best = fminf(best, r.cxx * dx * dx + 2.f * r.cxy * dx * dy + r.cyy * dy * dy);
+    }
+    return best < 1.01f;
 }
 
 // Issues the bulk copies of batch [bs, bs+cnt) into buffer `buf` (thread 0).
@@ -203,20 +226,16 @@ __device__ __forceinline__ void build_masks(const GeoRec *batch, int cnt, int lo
         const int s = tid + half * NT;
         const bool valid = s < cnt;
         GeoRec r;
-        float ex = 0.f, ey = 0.f;
-        bool boxed = false;
+        bool pd = false;
         if (valid) {
             r = batch[s];
-            boxed = conic_box(r, ex, ey);
+            pd = conic_pd(r);
         }
         const int word = s >> 5;
         for (int w = 0; w < nw; ++w) {
             const float x0 = (float)(tile_x0 + (w % wpr) * 8) + 0.5f;
             const float y0 = (float)(tile_y0 + (w / wpr) * 8) + 0.5f;
-            bool ov = valid;
-            if (boxed)
-                ov = (r.x - ex <= x0 + 7.f) && (r.x + ex >= x0) && (r.y - ey <= y0 + 7.f) &&
-                     (r.y + ey >= y0);
+            bool ov = valid && ellipse_hits_box(r, pd, x0, y0);
             if (limit) ov = ov && (lo + s <= limit[w]);
             const uint32_t bits = __ballot_sync(0xffffffffu, ov);
             if (lane == 0) wmask[w * 2 * nw + word] = bits;
@@ -239,31 +258,48 @@ __device__ __forceinline__ void load_color(const float4 *scol4, const float *sco
     }
 }
 
-// One front-to-back blend step of one pixel (rasterize_to_pixels_fwd.cu:139-171).
-template <int CD>
-__device__ __forceinline__ void blend_one(const GeoRec &q, const float (&col)[CD], float px,
-                                          float py, float &T, float (&acc)[CD], int32_t &cur,
-                                          bool &done, int32_t idx, uint32_t &n_contrib) {
-    if (done) return;
-    const float dx = q.x - px, dy = q.y - py;
-    const float sigma = (q.cxx * dx * dx + q.cyy * dy * dy) + 2.f * q.cxy * dx * dy;
-    if (sigma < 0.f || sigma >= 1.f) return;
-    const float alpha = fminf(0.999f, q.opac * __powf(1.f - sigma, q.beta));
-    const float next_T = T * (1.f - alpha);
-    if (next_T <= 1e-4f) {
-        done = true;
-        return;
-    }
-    const float vis = alpha * T;
+// One front-to-back blend step of a thread's two pixels (column px, rows py0
+// and py0 + 1) over record q (rasterize_to_pixels_fwd.cu:139-171): skip when
+// sigma is outside [0, 1), alpha = min(0.999, opacity (1 - sigma)^beta), stop
+// (exclusively) once the transmittance would reach 1e-4.  sigma is written as
+// the reference writes it, so the shared products of the two pixels are formed
+// once; the rest is select-based so that a warp issues it once for both pixels
+// and all lanes.  Lanes whose record is skipped evaluate finite dummies that
+// the selects discard.
+template <int CD, bool COUNT>
+__device__ __forceinline__ void blend_pair(const GeoRec &q, const float (&col)[CD], float px,
+                                           float py0, float py1, float &T0, float &T1,
+                                           float (&acc0)[CD], float (&acc1)[CD], int32_t &cur0,
+                                           int32_t &cur1, bool &d0, bool &d1, int32_t idx,
+                                           uint32_t &n_contrib) {
+    const float dx = q.x - px, dy0 = q.y - py0, dy1 = q.y - py1;
+    const float s0 = (q.cxx * dx * dx + q.cyy * dy0 * dy0) + 2.f * q.cxy * dx * dy0;
+    const float s1 = (q.cxx * dx * dx + q.cyy * dy1 * dy1) + 2.f * q.cxy * dx * dy1;
+    const bool v0 = !d0 && !(s0 < 0.f || s0 >= 1.f);
+    const bool v1 = !d1 && !(s1 < 0.f || s1 >= 1.f);
+    if (!__any_sync(0xffffffffu, v0 || v1)) return;
+    const float a0 = fminf(0.999f, q.opac * __powf(v0 ? 1.f - s0 : 1.f, q.beta));
+    const float a1 = fminf(0.999f, q.opac * __powf(v1 ? 1.f - s1 : 1.f, q.beta));
+    const float n0 = T0 * (1.f - a0), n1 = T1 * (1.f - a1);
+    const bool t0 = v0 && n0 <= 1e-4f, t1 = v1 && n1 <= 1e-4f;
+    const bool b0 = v0 && !t0, b1 = v1 && !t1;
+    d0 = d0 || t0;
+    d1 = d1 || t1;
+    const float w0 = b0 ? a0 * T0 : 0.f, w1 = b1 ? a1 * T1 : 0.f;
 #pragma unroll
-    for (int k = 0; k < CD; ++k) acc[k] += col[k] * vis;
-    cur = idx;
-    T = next_T;
-    ++n_contrib;
+    for (int k = 0; k < CD; ++k) {
+        acc0[k] += col[k] * w0;
+        acc1[k] += col[k] * w1;
+    }
+    T0 = b0 ? n0 : T0;
+    T1 = b1 ? n1 : T1;
+    cur0 = b0 ? idx : cur0;
+    cur1 = b1 ? idx : cur1;
+    if (COUNT) n_contrib += (uint32_t)b0 + (uint32_t)b1;
 }
 
 // --------------------------------------------------------------- forward
-template <int CD, bool PACK>
+template <int CD, bool PACK, bool COUNT>
 __global__ void __launch_bounds__(512) raster_fwd_kernel(RasterArgs a) {
     extern __shared__ __align__(128) unsigned char sm[];
     const int NT = blockDim.x, nw = NT >> 5, BR = 2 * NT;
@@ -368,8 +404,8 @@ __global__ void __launch_bounds__(512) raster_fwd_kernel(RasterArgs a) {
                         const GeoRec q = batch[t];
                         float col[CD];
                         load_color<CD, PACK>(scol4, scol, buf * BR + t, col);
-                        blend_one<CD>(q, col, px, py0, T0, acc0, cur0, d0, bs + t, n_contrib);
-                        blend_one<CD>(q, col, px, py1, T1, acc1, cur1, d1, bs + t, n_contrib);
+                        blend_pair<CD, COUNT>(q, col, px, py0, py1, T0, T1, acc0, acc1, cur0,
+                                              cur1, d0, d1, bs + t, n_contrib);
                         if (__all_sync(0xffffffffu, d0 && d1)) {
                             warp_done = true;
                             break;
@@ -386,7 +422,7 @@ __global__ void __launch_bounds__(512) raster_fwd_kernel(RasterArgs a) {
                     atomicOr(a.status, DEV_ERR_WAIT_TIMEOUT);
     }
 
-    if (a.pair_count) {
+    if (COUNT) {
         const uint32_t w = __reduce_add_sync(0xffffffffu, n_contrib);
         if (lane == 0 && w) atomicAdd(a.pair_count, (unsigned long long)w);
     }
@@ -434,43 +470,73 @@ __device__ __forceinline__ void bwd_pix_init(BwdPix<CD> &s, const RasterArgs &a,
     s.S = 0.f;
 }
 
-// One back-to-front step of one pixel (rasterize_to_pixels_bwd.cu:158-247); adds
-// the pixel's gradient contributions into g = [v_xy(2), v_conic(3), v_opacity,
-// v_beta, v_color(CD)].  (1-sigma)^(beta-1) and ln(1-sigma) are formed from
-// (1-sigma)^beta and one base-2 logarithm.
+// One back-to-front step of one pixel (rasterize_to_pixels_bwd.cu:158-247),
+// select-based: `valid` lanes (inside, at or before their last contributor,
+// sigma in [0, 1)) add their contributions to
+//   g = [w (cxx dx + cxy dy), w (cxy dx + cyy dy), w dx^2, w dx dy, w dy^2,
+//        vis v_alpha, vis v_alpha log2(1 - sigma), fac v_colour (CD)]
+// with w = v_alpha (1 - sigma)^(beta - 1); the record's constant factors
+// (-2 opacity beta, -opacity beta, opacity ln 2) are applied once after the
+// warp reduction (record_scales).  Other lanes evaluate finite dummies
+// (1 - sigma replaced by 1) whose contributions the selects zero.
 template <int CD>
-__device__ __forceinline__ bool grad_one(const GeoRec &q, const float (&col)[CD], float px,
-                                         float py, int32_t idx, BwdPix<CD> &s,
-                                         float (&g)[7 + CD]) {
-    if (!s.inside || idx > s.bin) return false;
-    const float dx = q.x - px, dy = q.y - py;
-    const float sigma = (q.cxx * dx * dx + q.cyy * dy * dy) + 2.f * q.cxy * dx * dy;
-    if (sigma < 0.f || sigma >= 1.f) return false;
-    const float om = 1.f - sigma;
+__device__ __forceinline__ void grad_px(const GeoRec &q, const float (&col)[CD], float dx,
+                                        float dy, float sigma, bool valid, BwdPix<CD> &s,
+                                        float (&g)[7 + CD]) {
+    const float om = valid ? 1.f - sigma : 1.f;
     const float vis = __powf(om, q.beta);
     const float alpha = fminf(0.999f, q.opac * vis);
     const float ra = 1.0f / (1.0f - alpha);
-    s.T *= ra;
-    const float fac = alpha * s.T;
+    const float Tn = s.T * ra;
+    const float fac = valid ? alpha * Tn : 0.f;
     float cv = 0.f;
 #pragma unroll
     for (int k = 0; k < CD; ++k) {
         g[7 + k] += fac * s.vrc[k];
         cv += col[k] * s.vrc[k];
     }
-    const float v_alpha = s.T * cv + ra * (s.K - s.S);
-    if (q.opac * vis <= 0.999f) {
-        const float v_sigma = -v_alpha * q.opac * q.beta * __fdividef(vis, om);
-        g[2] += dx * dx * v_sigma;
-        g[3] += 2.f * dx * dy * v_sigma;
-        g[4] += dy * dy * v_sigma;
-        g[0] += 2.f * v_sigma * (q.cxx * dx + q.cxy * dy);
-        g[1] += 2.f * v_sigma * (q.cxy * dx + q.cyy * dy);
-        g[5] += vis * v_alpha;
-        g[6] += v_alpha * q.opac * vis * (__log2f(om) * 0.6931471805599453f);
-    }
+    const float v_alpha = (valid && q.opac * vis <= 0.999f) ? Tn * cv + ra * (s.K - s.S) : 0.f;
+    const float w = v_alpha * __fdividef(vis, om);
+    g[0] += w * (q.cxx * dx + q.cxy * dy);
+    g[1] += w * (q.cxy * dx + q.cyy * dy);
+    g[2] += w * (dx * dx);
+    g[3] += w * (dx * dy);
+    g[4] += w * (dy * dy);
+    const float u = vis * v_alpha;
+    g[5] += u;
+    g[6] += u * __log2f(om);
     s.S += fac * cv;
+    s.T = valid ? Tn : s.T;
+}
+
+// Both pixels of a thread against record q; returns whether any lane of the
+// warp had a valid pixel (and so whether g needs reducing).
+template <int CD>
+__device__ __forceinline__ bool grad_pair(const GeoRec &q, const float (&col)[CD], float px,
+                                          float py0, float py1, int32_t idx, BwdPix<CD> &s0,
+                                          BwdPix<CD> &s1, float (&g)[7 + CD]) {
+    const float dx = q.x - px, dy0 = q.y - py0, dy1 = q.y - py1;
+    const float sg0 = (q.cxx * dx * dx + q.cyy * dy0 * dy0) + 2.f * q.cxy * dx * dy0;
+    const float sg1 = (q.cxx * dx * dx + q.cyy * dy1 * dy1) + 2.f * q.cxy * dx * dy1;
+    const bool v0 = s0.inside && idx <= s0.bin && !(sg0 < 0.f || sg0 >= 1.f);
+    const bool v1 = s1.inside && idx <= s1.bin && !(sg1 < 0.f || sg1 >= 1.f);
+    if (!__any_sync(0xffffffffu, v0 || v1)) return false;
+#pragma unroll
+    for (int u = 0; u < 7 + CD; ++u) g[u] = 0.f;
+    grad_px<CD>(q, col, dx, dy0, sg0, v0, s0, g);
+    grad_px<CD>(q, col, dx, dy1, sg1, v1, s1, g);
     return true;
+}
+
+// Factor turning the reduced sum g[u] of a record into its gradient value u of
+// [v_xy(2), v_conic(3), v_opacity, v_beta, v_colour(CD)].
+__device__ __forceinline__ float record_scale(int u, float opac, float beta) {
+    const float ob = opac * beta;
+    if (u < 2) return -2.f * ob;
+    if (u == 3) return -2.f * ob;
+    if (u < 5) return -ob;
+    if (u == 6) return opac * 0.6931471805599453f;
+    return 1.f;
 }
 
 // Sums g[OFF .. OFF+REM) over the warp in power-of-two chunks and adds each
@@ -574,6 +640,12 @@ __global__ void __launch_bounds__(512) raster_bwd_kernel(RasterArgs a) {
         const GeoRec *batch = srec + buf * BR;
         const int32_t gid0 = (tid < cnt) ? batch[tid].gid : 0;
         const int32_t gid1 = (tid + NT < cnt) ? batch[tid + NT].gid : 0;
+        // per-slot opacity and beta for the flush (the buffer may be refilled
+        // while other threads still flush)
+        const float op0 = (tid < cnt) ? batch[tid].opac : 0.f;
+        const float be0 = (tid < cnt) ? batch[tid].beta : 0.f;
+        const float op1 = (tid + NT < cnt) ? batch[tid + NT].opac : 0.f;
+        const float be1 = (tid + NT < cnt) ? batch[tid + NT].beta : 0.f;
         build_masks(batch, cnt, lo, NT, nw, wpr, tx * a.TS, ty * a.TS, tid, lane, wmask, wbin);
         if (!PACK) {
 #pragma unroll
@@ -601,11 +673,7 @@ __global__ void __launch_bounds__(512) raster_bwd_kernel(RasterArgs a) {
                 float col[CD];
                 load_color<CD, PACK>(scol4, scol, buf * BR + t, col);
                 float g[NV];
-#pragma unroll
-                for (int u = 0; u < NV; ++u) g[u] = 0.f;
-                bool any = grad_one<CD>(q, col, px, py0, idx, s0, g);
-                any |= grad_one<CD>(q, col, px, py1, idx, s1, g);
-                if (!__any_sync(0xffffffffu, any)) continue;
+                if (!grad_pair<CD>(q, col, px, py0, py1, idx, s0, s1, g)) continue;
                 ReduceChunks<0, NV>::run(g, lane, gacc + t * NV);
                 if (lane == 0) touched[t] = 1;
             }
@@ -616,10 +684,11 @@ __global__ void __launch_bounds__(512) raster_bwd_kernel(RasterArgs a) {
             const int sl = tid + half * NT;
             if (sl < cnt && touched[sl]) {
                 const int64_t gg = half ? gid1 : gid0;
+                const float op = half ? op1 : op0, be = half ? be1 : be0;
                 float *ga = gacc + sl * NV;
 #pragma unroll
                 for (int u = 0; u < NV; ++u) {
-                    const float val = ga[u];
+                    const float val = ga[u] * record_scale(u, op, be);
                     if (val != 0.f) {
                         float *dst;
                         if (u < 2) dst = a.v_m2 + 2 * gg + u;
@@ -666,8 +735,9 @@ static int launch_pack(int64_t T, int64_t n_prims, const int32_t *fl, const floa
     const int blk = 256;
     const int64_t nblk = (T + blk - 1) / blk;
     const unsigned grid = (unsigned)(nblk < 152 * 16 ? nblk : 152 * 16);
-    pack_records_kernel<CD, PACK><<<grid, blk, 0, st>>>(T, n_prims, fl, m2, cn, op, be, col,
-                                                       recs, PACK ? rcols : nullptr, status);
+    UBS_TIMED("raster_pack", st,
+              pack_records_kernel<CD, PACK><<<grid, blk, 0, st>>>(
+                  T, n_prims, fl, m2, cn, op, be, col, recs, PACK ? rcols : nullptr, status));
     note_launch();
     return check_launch("pack_records");
 }
@@ -682,11 +752,13 @@ static int launch_blend(RasterArgs &a, cudaStream_t st) {
                                               "of shared memory", a.TS, CD, L.total);
     const unsigned nblocks = (unsigned)a.n_buckets;
     if (nblocks == 0) return UBS_OK;
-    auto k = BWD ? raster_bwd_kernel<CD, PACK> : raster_fwd_kernel<CD, PACK>;
+    auto k = BWD ? raster_bwd_kernel<CD, PACK>
+                 : (a.pair_count ? raster_fwd_kernel<CD, PACK, true>
+                                 : raster_fwd_kernel<CD, PACK, false>);
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total) !=
         cudaSuccess)
         return check_launch("raster smem attribute");
-    k<<<nblocks, NT, L.total, st>>>(a);
+    UBS_TIMED(BWD ? "raster_bwd" : "raster_fwd", st, k<<<nblocks, NT, L.total, st>>>(a));
     note_launch();
     return check_launch(BWD ? "raster_bwd" : "raster_fwd");
 }

@@ -531,21 +531,22 @@ int ubs_scene_forward(int32_t dim, int64_t N, const float *xyz, const float *mea
     a.bucket_counts = w.bucket_counts;
     a.status = &w.hdr->status;
     if (CN > 0) {
-        UBS_SCENE_DIM(dim, scene_prim_fwd_kernel<DD><<<grid_for(CN, 128), 128, 0, st>>>(a));
+        UBS_TIMED("scene_prim_fwd", st,
+                  UBS_SCENE_DIM(dim, scene_prim_fwd_kernel<DD><<<grid_for(CN, 128), 128, 0, st>>>(a)));
         note_launch();
         if (int e = check_launch("scene_prim_fwd")) return e;
     }
     if (int e = device_exclusive_scan<int32_t>(w.bucket_counts, w.offsets, n_buckets,
                                                w.block_sums, &w.hdr->total, st))
         return e;
-    note_launch(2);
     if (cudaMemcpyAsync(w.cursor, w.offsets, (size_t)n_buckets * 4, cudaMemcpyDeviceToDevice, st) !=
         cudaSuccess)
         return check_launch("scene cursor copy");
     if (CN > 0) {
-        scene_emit_kernel<<<grid_for(CN, 256), 256, 0, st>>>(
-            CN, N, w.recs, w.radius, w.depth, view_dims, tile_base, (float)tile_size, w.cursor,
-            w.keys, capacity, &w.hdr->status);
+        UBS_TIMED("scene_emit", st,
+                  scene_emit_kernel<<<grid_for(CN, 256), 256, 0, st>>>(
+                      CN, N, w.recs, w.radius, w.depth, view_dims, tile_base, (float)tile_size,
+                      w.cursor, w.keys, capacity, &w.hdr->status));
         note_launch();
         if (int e = check_launch("scene_emit")) return e;
     }
@@ -626,7 +627,8 @@ int ubs_scene_backward(int32_t dim, int64_t N, const float *xyz, const float *me
     a.g_beta = v_beta;
     a.g_rgb = v_rgb;
     a.exact = exact_cond_grad;
-    UBS_SCENE_DIM(dim, scene_prim_bwd_kernel<DD><<<grid_for(CN, 128), 128, 0, st>>>(a));
+    UBS_TIMED("scene_prim_bwd", st,
+              UBS_SCENE_DIM(dim, scene_prim_bwd_kernel<DD><<<grid_for(CN, 128), 128, 0, st>>>(a)));
     note_launch();
     return check_launch("scene_prim_bwd");
 }

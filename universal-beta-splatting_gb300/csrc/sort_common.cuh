@@ -117,12 +117,13 @@ inline int device_exclusive_scan(const int32_t *in, OutT *out, int64_t n, int64_
         return UBS_OK;
     }
     const int64_t nblocks = (n + SCAN_TILE - 1) / SCAN_TILE;
-    scan_blocks_kernel<OutT><<<(unsigned)nblocks, SCAN_THREADS, 0, st>>>(in, out, n, sums);
-    ::ubs::note_launch();
-    scan_sums_kernel<<<1, SCAN_THREADS, 0, st>>>(sums, nblocks, total);
-    ::ubs::note_launch();
-    if (nblocks > 1) scan_add_kernel<OutT><<<grid_for(n, 256), 256, 0, st>>>(out, n, sums);
-    ::ubs::note_launch();
+    UBS_TIMED("scan", st,
+              scan_blocks_kernel<OutT><<<(unsigned)nblocks, SCAN_THREADS, 0, st>>>(in, out, n,
+                                                                                  sums);
+              scan_sums_kernel<<<1, SCAN_THREADS, 0, st>>>(sums, nblocks, total);
+              if (nblocks > 1) scan_add_kernel<OutT><<<grid_for(n, 256), 256, 0, st>>>(out, n,
+                                                                                       sums));
+    ::ubs::note_launch(nblocks > 1 ? 3 : 2);
     return check_launch("exclusive scan");
 }
 
@@ -256,15 +257,17 @@ inline int launch_bucket_sort(int64_t n_buckets, const int32_t *offsets, const i
                               int32_t *n_big, Writer w, cudaStream_t st) {
     if (n_buckets <= 0 || cap <= 0) return UBS_OK;
     if (cudaMemsetAsync(n_big, 0, 4, st) != cudaSuccess) return check_launch("sort memset");
-    bucket_sort_small_kernel<Writer><<<(unsigned)n_buckets, SORT_THREADS, 0, st>>>(
-        n_buckets, offsets, T_dev, cap, keys, big_list, n_big, w);
+    UBS_TIMED("bucket_sort_small", st,
+              bucket_sort_small_kernel<Writer><<<(unsigned)n_buckets, SORT_THREADS, 0, st>>>(
+                  n_buckets, offsets, T_dev, cap, keys, big_list, n_big, w));
     note_launch();
     if (cap > SMALL_SEG) {
         const int64_t max_big = cap / (SMALL_SEG + 1);
         const unsigned grid = (unsigned)imin64(imin64(max_big, n_buckets), 304);
         if (grid > 0) {
-            bucket_sort_big_kernel<Writer><<<grid, BIG_THREADS, 0, st>>>(
-                n_buckets, offsets, T_dev, cap, keys, scratch, big_list, n_big, w);
+            UBS_TIMED("bucket_sort_big", st,
+                      bucket_sort_big_kernel<Writer><<<grid, BIG_THREADS, 0, st>>>(
+                          n_buckets, offsets, T_dev, cap, keys, scratch, big_list, n_big, w));
             note_launch();
         }
     }

@@ -15,6 +15,23 @@ int check_launch(const char *what);
 // Counts kernel launches made by this library (read with ubs_launch_count).
 void note_launch(int n = 1);
 
+// Opt-in kernel timing (ubs_profile_start / _stop): while enabled, a
+// KernelTimer records a CUDA event before its launch and one after it, on the
+// launching stream; otherwise it does nothing.
+struct KernelTimer {
+    int slot;
+    cudaStream_t st;
+    KernelTimer(const char *name, cudaStream_t s);
+    ~KernelTimer();
+};
+
+// Launch statement(s) timed as one kernel under `name` when timing is enabled.
+#define UBS_TIMED(name, st, ...)                                                \
+    do {                                                                        \
+        ::ubs::KernelTimer ubs_kt_(name, st);                                   \
+        __VA_ARGS__;                                                            \
+    } while (0)
+
 #define UBS_REQUIRE(cond, ...)                                                  \
     do {                                                                        \
         if (!(cond)) return ::ubs::set_error(UBS_ERR_INVALID, __VA_ARGS__);     \

@@ -63,6 +63,10 @@ SIGNATURES = {
     "ubs_scene_backward": ([_I32, _I64] + [_P] * 7 + [_I32] + [_P] * 7 + [_I32, _I32, _F, _F, _F, _F]
                            + [_P] * 5 + [_P] * 7 + [_I32, _I64, _P, _SZ, _P], _INT),
     "ubs_scene_stats": ([_P, _I64P, _U32P, _P], _INT),
+    "ubs_profile_start": ([_I32], _INT),
+    "ubs_profile_stop": ([ctypes.POINTER(_I32)], _INT),
+    "ubs_profile_result": ([_I32, ctypes.POINTER(ctypes.c_char_p), _I64P,
+                            ctypes.POINTER(ctypes.c_double)], _INT),
     "ubs_fp32_probe_workspace_bytes": ([], _SZ),
     "ubs_fp32_probe": ([_I32, _P, _SZ, ctypes.POINTER(ctypes.c_double), _P], _INT),
 }
@@ -129,6 +133,24 @@ def stop_timing():
     for name, e0, e1 in rec:
         n, t = out.get(name, (0, 0.0))
         out[name] = (n + 1, t + e0.elapsed_time(e1))
+    return out
+
+
+def profile_start(max_launches=4096):
+    """Time every kernel the library launches from now on (CUDA events on the
+    launching stream)."""
+    call("ubs_profile_start", int(max_launches))
+
+
+def profile_stop():
+    """Stop kernel timing; returns {kernel: (launches, total ms)}."""
+    n = ctypes.c_int32(0)
+    call("ubs_profile_stop", ctypes.byref(n))
+    out = {}
+    for i in range(n.value):
+        name, cnt, ms = ctypes.c_char_p(), ctypes.c_int64(), ctypes.c_double()
+        call("ubs_profile_result", i, ctypes.byref(name), ctypes.byref(cnt), ctypes.byref(ms))
+        out[name.value.decode()] = (int(cnt.value), float(ms.value))
     return out
 
 
