@@ -183,10 +183,13 @@ def test_isect_bit_exact(C, N, W, H, ts):
     np.testing.assert_array_equal(npy(fl_u), fl_uo)
 
 
-def test_isect_long_buckets_and_empty():
-    """Buckets longer than the shared-memory sort (4096) take the merge path."""
+@pytest.mark.parametrize("N", [700, 2500, 30000])
+def test_isect_long_buckets_and_empty(N):
+    """Every primitive covers every tile, so each bucket holds N keys: 700 are
+    sorted by one warp in registers, 2500 by one CTA in shared memory, 30000
+    (longer than 4096) on the merge path."""
     from gsplat.cuda._wrapper import isect_offset_encode, isect_tiles
-    N, W, H, ts = 30000, 64, 64, 16
+    W, H, ts = 64, 64, 16
     g = torch.Generator().manual_seed(11)
     m2 = torch.rand(1, N, 2, generator=g) * 64
     radii = torch.full((1, N), 100, dtype=torch.int32)  # every primitive covers every tile

@@ -27,7 +27,9 @@ struct IsectHeader {
     int64_t total;     // number of intersections
     uint32_t status;   // DeviceError bits
     int32_t n_big;     // number of buckets longer than SMALL_SEG
-    int64_t pad[6];
+    int32_t n_mid;     // number of buckets longer than WARP_SEG, at most SMALL_SEG
+    int32_t pad0;
+    int64_t pad[5];
 };
 static_assert(sizeof(IsectHeader) <= 256, "header too large");
 

@@ -61,6 +61,7 @@ struct RasterArgs {
     const int64_t *v_pix_base;  // [C] first pixel of each view in the image buffer
     int32_t n_buckets;          // total (view, tile) buckets
     const int64_t *n_isects_dev; // device-side intersection count (nullptr: n_isects)
+    const int32_t *order;        // CTA -> bucket launch order (nullptr: identity)
 };
 
 // Where a (view, tile) bucket lives: view, tile within the view, image size,
@@ -311,7 +312,7 @@ __global__ void __launch_bounds__(512) raster_fwd_kernel(RasterArgs a) {
     float *scol = reinterpret_cast<float *>(sm + L.col_off);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int bt = blockIdx.x;
+    const int bt = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;
     const TileLoc loc = locate_tile(a, bt);
     const int cam = loc.cam;
     const int ty = loc.tile / loc.TW, tx = loc.tile - ty * loc.TW;
@@ -575,7 +576,7 @@ __global__ void __launch_bounds__(512) raster_bwd_kernel(RasterArgs a) {
     int32_t *touched = reinterpret_cast<int32_t *>(sm + L.touched_off);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int bt = blockIdx.x;
+    const int bt = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;
     if (a.masks && !a.masks[bt]) return;
     const TileLoc loc = locate_tile(a, bt);
     const int cam = loc.cam;
@@ -841,12 +842,14 @@ static void fill_common(RasterArgs &a, int32_t C, int64_t N, int32_t ch, int64_t
     a.v_pix_base = nullptr;
     a.n_buckets = C * tw * th;
     a.n_isects_dev = nullptr;
+    a.order = nullptr;
 }
 
 // Blend of the fused multi-view path (scene.cu): 3 colour channels packed
 // with the records, per-view grids, intersection count read on the device.
 int scene_blend(int fwd, int32_t C, int64_t CN, int32_t n_buckets, int32_t tile_size,
-                const int32_t *offsets, const int64_t *T_dev, int64_t cap, const void *recs,
+                const int32_t *offsets, const int32_t *order, const int64_t *T_dev, int64_t cap,
+                const void *recs,
                 const float4 *rcols, const float *bg, const int32_t *tile_base,
                 const int32_t *dims, const int64_t *pix_base, float *out_c, float *out_a,
                 int32_t *last_ids, const float *render_alphas, const int32_t *last_in,
@@ -867,6 +870,7 @@ int scene_blend(int fwd, int32_t C, int64_t CN, int32_t n_buckets, int32_t tile_
     a.v_pix_base = pix_base;
     a.n_buckets = n_buckets;
     a.n_isects_dev = T_dev;
+    a.order = order;
     if (fwd) {
         a.out_c = out_c;
         a.out_a = out_a;

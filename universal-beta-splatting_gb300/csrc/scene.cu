@@ -31,7 +31,8 @@ namespace ubs {
 
 // raster.cu: the blend kernels in multi-view mode over sorted packed records
 int scene_blend(int fwd, int32_t C, int64_t CN, int32_t n_buckets, int32_t tile_size,
-                const int32_t *offsets, const int64_t *T_dev, int64_t cap, const void *recs,
+                const int32_t *offsets, const int32_t *order, const int64_t *T_dev, int64_t cap,
+                const void *recs,
                 const float4 *rcols, const float *bg, const int32_t *tile_base,
                 const int32_t *dims, const int64_t *pix_base, float *out_c, float *out_a,
                 int32_t *last_ids, const float *render_alphas, const int32_t *last_in,
@@ -51,8 +52,10 @@ struct __align__(16) Rec {
 struct SceneHeader {
     int64_t total;   // intersections counted on the device
     uint32_t status; // DeviceError bits
-    int32_t n_big;
-    int64_t pad[6];
+    int32_t n_big;   // buckets longer than SMALL_SEG
+    int32_t n_mid;   // buckets longer than WARP_SEG, at most SMALL_SEG
+    int32_t pad0;
+    int64_t pad[5];
 };
 
 struct SceneArgs {
@@ -229,6 +232,11 @@ template <int D> __global__ void scene_prim_fwd_kernel(SceneArgs a) {
         for (uint32_t x = x0; x < x1; ++x) atomicAdd(&bc[y * TW + x], 1);
 }
 
+// Writes one sort key per (view, primitive, tile) at the tile's cursor.  A
+// warp flattens the tile rectangles of its 32 (view, primitive) entries into
+// one list of (entry, tile) pairs and emits 32 pairs per round, so a warp's
+// rounds follow the warp's total tile count rather than its largest entry and
+// the 32 cursor atomics of a round are independent.
 __global__ void scene_emit_kernel(int64_t CN, int64_t N, const Rec *__restrict__ recs,
                                   const int32_t *__restrict__ radius,
                                   const float *__restrict__ depth,
@@ -237,25 +245,59 @@ __global__ void scene_emit_kernel(int64_t CN, int64_t N, const Rec *__restrict__
                                   int32_t *__restrict__ cursor, uint64_t *__restrict__ keys,
                                   int64_t cap, uint32_t *status) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= CN) return;
-    const int32_t rad = radius[idx];
-    if (rad <= 0) return;
-    const int v = (int)(idx / N);
-    const uint32_t TW = (uint32_t)dims[v * 4 + 2], TH = (uint32_t)dims[v * 4 + 3];
-    const float4 xy = reinterpret_cast<const float4 *>(recs + idx)[0];
-    const float rr = (float)rad / ts, tx = xy.x / ts, ty = xy.y / ts;
-    const uint32_t x0 = min(max(0u, __float2uint_rz(floorf(tx - rr))), TW);
-    const uint32_t y0 = min(max(0u, __float2uint_rz(floorf(ty - rr))), TH);
-    const uint32_t x1 = min(max(0u, __float2uint_rz(ceilf(tx + rr))), TW);
-    const uint32_t y1 = min(max(0u, __float2uint_rz(ceilf(ty + rr))), TH);
-    const uint64_t key = ((uint64_t)(uint32_t)__float_as_int(depth[idx]) << 32) | (uint64_t)idx;
-    int32_t *cur = cursor + tile_base[v];
-    for (uint32_t y = y0; y < y1; ++y)
-        for (uint32_t x = x0; x < x1; ++x) {
-            const int32_t pos = atomicAdd(&cur[y * TW + x], 1);
-            if (pos >= 0 && pos < cap) keys[pos] = key;
+    const int lane = threadIdx.x & 31;
+    uint32_t bw = 1, n = 0, pitch = 0;
+    int32_t *cur = cursor;
+    uint64_t key = 0;
+    if (idx < CN && radius[idx] > 0) {
+        const int v = (int)(idx / N);
+        const uint32_t TW = (uint32_t)dims[v * 4 + 2], TH = (uint32_t)dims[v * 4 + 3];
+        const float4 xy = reinterpret_cast<const float4 *>(recs + idx)[0];
+        const float rr = (float)radius[idx] / ts, tx = xy.x / ts, ty = xy.y / ts;
+        const uint32_t x0 = min(max(0u, __float2uint_rz(floorf(tx - rr))), TW);
+        const uint32_t y0 = min(max(0u, __float2uint_rz(floorf(ty - rr))), TH);
+        const uint32_t x1 = min(max(0u, __float2uint_rz(ceilf(tx + rr))), TW);
+        const uint32_t y1 = min(max(0u, __float2uint_rz(ceilf(ty + rr))), TH);
+        if (x1 > x0 && y1 > y0) {
+            bw = x1 - x0;
+            n = bw * (y1 - y0);
+            cur = cursor + tile_base[v] + (int64_t)y0 * TW + x0;
+            key = ((uint64_t)(uint32_t)__float_as_int(depth[idx]) << 32) | (uint64_t)idx;
+            pitch = TW;
+        }
+    }
+    // inclusive scan of the pair counts over the warp
+    uint32_t incl = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t j = base + lane;
+        // owner: first lane whose inclusive count exceeds j
+        int owner = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+            const uint32_t c = __shfl_sync(0xffffffffu, incl, owner + step - 1);
+            if (c <= j) owner += step;
+        }
+        const uint32_t o_incl = __shfl_sync(0xffffffffu, incl, owner);
+        const uint32_t o_n = __shfl_sync(0xffffffffu, n, owner);
+        const uint32_t o_bw = __shfl_sync(0xffffffffu, bw, owner);
+        const uint32_t o_pitch = __shfl_sync(0xffffffffu, pitch, owner);
+        const uint64_t o_key = __shfl_sync(0xffffffffu, key, owner);
+        int32_t *o_cur = reinterpret_cast<int32_t *>(
+            __shfl_sync(0xffffffffu, reinterpret_cast<uintptr_t>(cur), owner));
+        if (j < total) {
+            const uint32_t local = j - (o_incl - o_n);
+            const uint32_t ry = local / o_bw, rx = local - ry * o_bw;
+            const int32_t pos = atomicAdd(o_cur + (int64_t)ry * o_pitch + rx, 1);
+            if (pos >= 0 && pos < cap) keys[pos] = o_key;
             else atomicOr(status, DEV_ERR_OVERFLOW);
         }
+    }
 }
 
 // Sorted-entry writer of the fused path: the blend's packed record and colour.
@@ -404,7 +446,7 @@ struct SceneWs {
     Rec *recs;
     int32_t *radius;
     float *depth;
-    int32_t *bucket_counts, *offsets, *cursor, *big_list;
+    int32_t *bucket_counts, *offsets, *cursor, *big_list, *order;
     int64_t *block_sums;
     uint64_t *keys, *scratch;
     Rec *sorted;
@@ -431,6 +473,7 @@ SceneWs scene_ws(void *base, int32_t C, int64_t N, int32_t nb, int64_t cap) {
     w.offsets = reinterpret_cast<int32_t *>(take((size_t)(nb + 1) * 4));
     w.cursor = reinterpret_cast<int32_t *>(take((size_t)nb * 4));
     w.big_list = reinterpret_cast<int32_t *>(take((size_t)nb * 4));
+    w.order = reinterpret_cast<int32_t *>(take((size_t)nb * 4));
     w.block_sums = reinterpret_cast<int64_t *>(take(((nb + SCAN_TILE - 1) / SCAN_TILE + 1) * 8));
     w.keys = reinterpret_cast<uint64_t *>(take(cap * 8));
     w.scratch = reinterpret_cast<uint64_t *>(take(cap * 8));
@@ -554,7 +597,12 @@ int ubs_scene_forward(int32_t dim, int64_t N, const float *xyz, const float *mea
     if (int e = launch_bucket_sort(n_buckets, w.offsets, &w.hdr->total, capacity, w.keys,
                                    w.scratch, w.big_list, &w.hdr->n_big, wr, st))
         return e;
-    return scene_blend(1, C, CN, n_buckets, tile_size, w.offsets, &w.hdr->total, capacity,
+    UBS_TIMED("bucket_order", st,
+              bucket_order_kernel<<<1, 1024, 0, st>>>(w.offsets, &w.hdr->total, capacity,
+                                                      n_buckets, w.order));
+    note_launch();
+    if (int e = check_launch("bucket_order")) return e;
+    return scene_blend(1, C, CN, n_buckets, tile_size, w.offsets, w.order, &w.hdr->total, capacity,
                        w.sorted, w.cols, backgrounds, tile_base, view_dims, pix_base,
                        render_colors, render_alphas, last_ids, nullptr, nullptr, nullptr, nullptr,
                        nullptr, nullptr, nullptr, nullptr, nullptr, &w.hdr->status, st);
@@ -594,7 +642,8 @@ int ubs_scene_backward(int32_t dim, int64_t N, const float *xyz, const float *me
           *v_be = v_op + CN;
     if (cudaMemsetAsync(w.grads, 0, CN * 10 * 4, st) != cudaSuccess)
         return check_launch("scene_backward memset");
-    if (int e = scene_blend(0, C, CN, n_buckets, tile_size, w.offsets, &w.hdr->total, capacity,
+    if (int e = scene_blend(0, C, CN, n_buckets, tile_size, w.offsets, w.order, &w.hdr->total,
+                            capacity,
                             w.sorted, w.cols, backgrounds, tile_base, view_dims, pix_base,
                             nullptr, nullptr, nullptr, render_alphas, last_ids, v_render_colors,
                             v_render_alphas, v_m2, v_cn, v_col, v_op, v_be, &w.hdr->status, st))

@@ -10,7 +10,8 @@ namespace ubs {
 constexpr int SCAN_ITEMS = 4;
 constexpr int SCAN_THREADS = 1024;
 constexpr int SCAN_TILE = SCAN_ITEMS * SCAN_THREADS;
-constexpr int SMALL_SEG = 4096; // longest bucket sorted in shared memory
+constexpr int WARP_SEG = 1024;  // longest bucket sorted by one warp in registers
+constexpr int SMALL_SEG = 4096; // longest bucket sorted by one CTA in shared memory
 constexpr int SORT_THREADS = 256;
 constexpr int BIG_THREADS = 1024;
 constexpr int MERGE_ITEMS = 8;
@@ -162,27 +163,165 @@ __device__ __forceinline__ void bucket_range(const int32_t *offsets, int64_t bkt
     if (hi < lo) hi = lo;
 }
 
+// Heaviest-first order of the buckets for the blend (longest-processing-time
+// scheduling): one CTA counting-sorts the buckets by record count into
+// ORDER_BINS bins of 4 records (descending; counts >= 4 * ORDER_BINS share the
+// first bin).  Order within a bin is arbitrary, which only changes the launch
+// order of the blend's CTAs, never a result.
+constexpr int ORDER_BINS = 1024;
+static __global__ void __launch_bounds__(1024) bucket_order_kernel(const int32_t *__restrict__ offsets,
+                                                            const int64_t *T_dev, int64_t cap,
+                                                            int32_t n_buckets,
+                                                            int32_t *__restrict__ order) {
+    __shared__ int32_t bins[ORDER_BINS];
+    __shared__ int32_t warp_tot[32];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int64_t T = T_dev ? imin64(*T_dev, cap) : cap;
+    for (int i = tid; i < ORDER_BINS; i += blockDim.x) bins[i] = 0;
+    __syncthreads();
+    auto bin_of = [&](int32_t b) {
+        int64_t lo, hi;
+        bucket_range(offsets, b, n_buckets, T, lo, hi);
+        const int64_t c = (hi - lo) >> 2;
+        return ORDER_BINS - 1 - (int)(c < ORDER_BINS - 1 ? c : ORDER_BINS - 1);
+    };
+    for (int32_t b = tid; b < n_buckets; b += blockDim.x) atomicAdd(&bins[bin_of(b)], 1);
+    __syncthreads();
+    // exclusive scan of the 1024 bins (one per thread)
+    const int v = tid < ORDER_BINS ? bins[tid] : 0;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int t = warp_tot[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        warp_tot[lane] = t; // inclusive
+    }
+    __syncthreads();
+    if (tid < ORDER_BINS) bins[tid] = x - v + (wid ? warp_tot[wid - 1] : 0);
+    __syncthreads();
+    for (int32_t b = tid; b < n_buckets; b += blockDim.x) order[atomicAdd(&bins[bin_of(b)], 1)] = b;
+}
+
+// Bitonic sort of the 32 * E keys of a warp held E per lane in registers,
+// blocked (element i = lane * E + e): exchange distances below E stay inside
+// a lane, larger ones are lane-xor shuffles.  Fully unrolled, so the key
+// arrays stay in registers.
+template <int E>
+__device__ __forceinline__ void warp_bitonic(uint64_t (&v)[E], int lane) {
+    constexpr int N = 32 * E;
+#pragma unroll
+    for (int k = 2; k <= N; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j < E) {
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    const int p = e ^ j;
+                    if (p > e) {
+                        const bool up = (((lane * E + e) & k) == 0);
+                        const uint64_t a = v[e], b = v[p];
+                        const bool sw = (a > b) == up;
+                        v[e] = sw ? b : a;
+                        v[p] = sw ? a : b;
+                    }
+                }
+            } else {
+                const int lj = j / E;
+                const bool lower = (lane & lj) == 0;
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    const uint64_t o = __shfl_xor_sync(0xffffffffu, v[e], lj);
+                    const bool up = (((lane * E + e) & k) == 0);
+                    const bool keep_min = lower == up;
+                    const bool o_less = o < v[e];
+                    v[e] = (keep_min == o_less) ? o : v[e];
+                }
+            }
+        }
+    }
+}
+
+template <int E, typename Writer>
+__device__ __forceinline__ void warp_sort_bucket(const uint64_t *__restrict__ keys, int64_t lo,
+                                                 int n, int64_t bkt, int lane, const Writer &w) {
+    uint64_t v[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int i = lane * E + e;
+        v[e] = i < n ? keys[lo + i] : ~0ull;
+    }
+    warp_bitonic<E>(v, lane);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int i = lane * E + e;
+        if (i < n) w(v[e], lo + i, bkt);
+    }
+}
+
+// One warp per bucket for buckets of at most WARP_SEG keys (padded to the
+// next power of two >= 32 with all-ones keys, which sort last); longer
+// buckets go to the device-side lists: mid (<= SMALL_SEG) from the front of
+// `lists`, big from the back.  counters = {n_big, n_mid}.
 template <typename Writer>
-__global__ void __launch_bounds__(SORT_THREADS) bucket_sort_small_kernel(
+__global__ void __launch_bounds__(256) bucket_sort_warp_kernel(
     int64_t n_buckets, const int32_t *__restrict__ offsets, const int64_t *T_dev, int64_t cap,
-    const uint64_t *__restrict__ keys, int32_t *big_list, int32_t *n_big, Writer w) {
-    __shared__ uint64_t s[SMALL_SEG];
-    const int64_t bkt = blockIdx.x;
+    const uint64_t *__restrict__ keys, int32_t *lists, int32_t *counters, Writer w) {
+    const int lane = threadIdx.x & 31;
+    const int64_t bkt = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (bkt >= n_buckets) return;
     const int64_t T = T_dev ? imin64(*T_dev, cap) : cap;
     int64_t lo, hi;
     bucket_range(offsets, bkt, n_buckets, T, lo, hi);
-    const int n = (int)(hi - lo);
+    const int64_t n = hi - lo;
     if (n <= 0) return;
-    if (n > SMALL_SEG) {
-        if (threadIdx.x == 0) big_list[atomicAdd(n_big, 1)] = (int32_t)bkt;
+    if (n > WARP_SEG) {
+        if (lane == 0) {
+            if (n > SMALL_SEG) lists[n_buckets - 1 - atomicAdd(&counters[0], 1)] = (int32_t)bkt;
+            else lists[atomicAdd(&counters[1], 1)] = (int32_t)bkt;
+        }
         return;
     }
-    int n2 = 1;
-    while (n2 < n) n2 <<= 1;
-    for (int i = threadIdx.x; i < n2; i += blockDim.x) s[i] = i < n ? keys[lo + i] : ~0ull;
-    __syncthreads();
-    block_bitonic(s, n2);
-    for (int i = threadIdx.x; i < n; i += blockDim.x) w(s[i], lo + i, bkt);
+    const int m = (int)n;
+    if (m <= 32) warp_sort_bucket<1>(keys, lo, m, bkt, lane, w);
+    else if (m <= 64) warp_sort_bucket<2>(keys, lo, m, bkt, lane, w);
+    else if (m <= 128) warp_sort_bucket<4>(keys, lo, m, bkt, lane, w);
+    else if (m <= 256) warp_sort_bucket<8>(keys, lo, m, bkt, lane, w);
+    else if (m <= 512) warp_sort_bucket<16>(keys, lo, m, bkt, lane, w);
+    else warp_sort_bucket<32>(keys, lo, m, bkt, lane, w);
+}
+
+// Buckets of WARP_SEG < n <= SMALL_SEG keys (the mid list): a fixed grid walks
+// the device-side list; one CTA sorts a bucket in shared memory.
+template <typename Writer>
+__global__ void __launch_bounds__(SORT_THREADS) bucket_sort_mid_kernel(
+    int64_t n_buckets, const int32_t *__restrict__ offsets, const int64_t *T_dev, int64_t cap,
+    const uint64_t *__restrict__ keys, const int32_t *lists, const int32_t *counters, Writer w) {
+    __shared__ uint64_t s[SMALL_SEG];
+    const int n_mid = counters[1];
+    const int64_t T = T_dev ? imin64(*T_dev, cap) : cap;
+    for (int item = blockIdx.x; item < n_mid; item += gridDim.x) {
+        __syncthreads();
+        const int64_t bkt = lists[item];
+        int64_t lo, hi;
+        bucket_range(offsets, bkt, n_buckets, T, lo, hi);
+        const int n = (int)(hi - lo);
+        int n2 = 1;
+        while (n2 < n) n2 <<= 1;
+        for (int i = threadIdx.x; i < n2; i += blockDim.x) s[i] = i < n ? keys[lo + i] : ~0ull;
+        __syncthreads();
+        block_bitonic(s, n2);
+        for (int i = threadIdx.x; i < n; i += blockDim.x) w(s[i], lo + i, bkt);
+    }
 }
 
 // merge path: number of elements taken from a for output diagonal d
@@ -203,13 +342,13 @@ __device__ __forceinline__ int64_t merge_split(const uint64_t *a, int64_t na, co
 template <typename Writer>
 __global__ void __launch_bounds__(BIG_THREADS) bucket_sort_big_kernel(
     int64_t n_buckets, const int32_t *__restrict__ offsets, const int64_t *T_dev, int64_t cap,
-    uint64_t *keys, uint64_t *scratch, const int32_t *big_list, const int32_t *n_big_ptr, Writer w) {
+    uint64_t *keys, uint64_t *scratch, const int32_t *lists, const int32_t *counters, Writer w) {
     __shared__ uint64_t s[SMALL_SEG];
-    const int n_big = *n_big_ptr;
+    const int n_big = counters[0];
     const int64_t T = T_dev ? imin64(*T_dev, cap) : cap;
     for (int item = blockIdx.x; item < n_big; item += gridDim.x) {
         __syncthreads();
-        const int64_t bkt = big_list[item];
+        const int64_t bkt = lists[n_buckets - 1 - item];
         int64_t lo, hi;
         bucket_range(offsets, bkt, n_buckets, T, lo, hi);
         const int64_t n = hi - lo;
@@ -249,25 +388,35 @@ __global__ void __launch_bounds__(BIG_THREADS) bucket_sort_big_kernel(
     }
 }
 
-// Launches the per-bucket sort: small buckets in shared memory, long ones on
-// a fixed grid.  big_list / n_big are scratch (n_big is zeroed here).
+// Launches the per-bucket sort: buckets of <= WARP_SEG keys one warp each in
+// registers, <= SMALL_SEG one CTA each in shared memory, longer ones merged on
+// a fixed grid.  lists ([n_buckets]) and counters ([2], zeroed here) are
+// scratch.
 template <typename Writer>
 inline int launch_bucket_sort(int64_t n_buckets, const int32_t *offsets, const int64_t *T_dev,
-                              int64_t cap, uint64_t *keys, uint64_t *scratch, int32_t *big_list,
-                              int32_t *n_big, Writer w, cudaStream_t st) {
+                              int64_t cap, uint64_t *keys, uint64_t *scratch, int32_t *lists,
+                              int32_t *counters, Writer w, cudaStream_t st) {
     if (n_buckets <= 0 || cap <= 0) return UBS_OK;
-    if (cudaMemsetAsync(n_big, 0, 4, st) != cudaSuccess) return check_launch("sort memset");
-    UBS_TIMED("bucket_sort_small", st,
-              bucket_sort_small_kernel<Writer><<<(unsigned)n_buckets, SORT_THREADS, 0, st>>>(
-                  n_buckets, offsets, T_dev, cap, keys, big_list, n_big, w));
+    if (cudaMemsetAsync(counters, 0, 8, st) != cudaSuccess) return check_launch("sort memset");
+    UBS_TIMED("bucket_sort_warp", st,
+              bucket_sort_warp_kernel<Writer><<<grid_for(n_buckets, 8), 256, 0, st>>>(
+                  n_buckets, offsets, T_dev, cap, keys, lists, counters, w));
     note_launch();
+    if (cap > WARP_SEG) {
+        const int64_t max_mid = cap / (WARP_SEG + 1);
+        const unsigned grid = (unsigned)imin64(imin64(max_mid, n_buckets), 152 * 6);
+        UBS_TIMED("bucket_sort_mid", st,
+                  bucket_sort_mid_kernel<Writer><<<grid, SORT_THREADS, 0, st>>>(
+                      n_buckets, offsets, T_dev, cap, keys, lists, counters, w));
+        note_launch();
+    }
     if (cap > SMALL_SEG) {
         const int64_t max_big = cap / (SMALL_SEG + 1);
         const unsigned grid = (unsigned)imin64(imin64(max_big, n_buckets), 304);
         if (grid > 0) {
             UBS_TIMED("bucket_sort_big", st,
                       bucket_sort_big_kernel<Writer><<<grid, BIG_THREADS, 0, st>>>(
-                          n_buckets, offsets, T_dev, cap, keys, scratch, big_list, n_big, w));
+                          n_buckets, offsets, T_dev, cap, keys, scratch, lists, counters, w));
             note_launch();
         }
     }
