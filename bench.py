@@ -51,12 +51,14 @@ WORKLOAD = ("1M 6-D Beta primitives, 1920x1080 (fx=fy=1500), radius-4 orbit came
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n-prims", type=int, default=N_PRIMS)
     ap.add_argument("--no-ref-gpu", action="store_true", help="skip timing the reference kernels")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the batched (C, D) and serving (E) configurations")
     ap.add_argument("--profile", action="store_true",
                     help="run only the fused step (first frame, --warmup steps, one more step) "
                          "for an ncu capture; prints no JSON line")
@@ -261,6 +263,177 @@ def read_profile_traffic(kernel):
             except ValueError:
                 return None
     return None
+
+
+# --------------------------------------------- batched and served configs
+def _ref_pipeline():
+    try:
+        import ref_gpu as RG
+        return RG.RefPipeline() if RG.available() else None
+    except Exception:  # noqa: BLE001
+        return None
+
+
+class TrainViews:
+    """Fused forward + L1 + backward over all views in one launch."""
+
+    def __init__(self, p, cams, dev, tile):
+        from ubs.render import Renderer, Views
+        self.p = p
+        self.r = Renderer(dim=p["scale"].shape[1], tile_size=tile)
+        self.views = Views(cams, tile_size=tile, device=dev)
+        g = torch.Generator().manual_seed(3)
+        self.target = torch.rand(self.views.n_pixels, 3, generator=g).to(dev)
+        self.bg = torch.zeros(len(cams), 3, device=dev)
+        with torch.no_grad():
+            self.r.render(p, self.views, self.bg, check=True)
+
+    def step(self):
+        for v in self.p.values():
+            v.grad = None
+        colors, _ = self.r.render(self.p, self.views, self.bg, check=False)
+        (colors - self.target).abs().mean().backward()
+
+
+def _train_views(p, cams, dev, tile, reps, flush):
+    """ms per fused step (after two warm-up steps) and the intersection count."""
+    tv = TrainViews(p, cams, dev, tile)
+    for _ in range(2):
+        tv.step()
+    ms = time_steps(tv.step, reps, dev, flush)
+    tv.r._check_pending()
+    return ms, tv.r.last_isects
+
+
+def _ref_train_views(rp, p, cams, dev, reps, flush):
+    """ms per step of the reference's kernels, one view per launch."""
+    ri, rj = None, None
+    from ubs import scene as S
+    ri, rj = S.rest_indices(p["scale"].shape[1], dev)
+    g = torch.Generator().manual_seed(3)
+    targets = [torch.rand(3, c.height, c.width, generator=g).to(dev) for c in cams]
+    bg = torch.zeros(3, device=dev)
+
+    def step():
+        for v in p.values():
+            v.grad = None
+        for c, t in zip(cams, targets):
+            img, _, _ = rp.render_view(p, c.viewmat, c.K, c.width, c.height, c.center, bg, ri, rj,
+                                       tile_size=TILE, timestamp=c.timestamp)
+            ((img - t).abs().mean() / len(cams)).backward()
+
+    step()
+    return time_steps(step, reps, dev, flush)
+
+
+def run_config_c(dev, flush, rp):
+    """500k 7-D dynamic primitives, 8 views of 1352x1014 with timestamps, one
+    batched forward + backward."""
+    from ubs import scene as S
+    p = S.synthetic_params(500_000, 7, seed=0, xyz_range=2.0, device=dev)
+    for v in p.values():
+        v.requires_grad_(True)
+    rng = np.random.default_rng(0)
+    cams = [S.orbit_view(100 + i, 4.0, 1352, 1014, 1056.25, 1056.25,
+                         timestamp=float(rng.uniform()), device=dev) for i in range(8)]
+    ms, isects = _train_views(p, cams, dev, TILE, 10, flush)
+    out = {"workload": "500k 7-D primitives, 8 views 1352x1014 (fx=fy=1056.25) with timestamps "
+                       "U[0,1], one fused forward + L1 + backward", "ms_per_step": ms,
+           "it_per_s": 1000.0 / ms, "views_per_s": 8000.0 / ms, "isects": isects}
+    if rp is not None:
+        r_ms = _ref_train_views(rp, p, cams, dev, 3, flush)
+        out["ref_gpu_plain"] = {"ms_per_step": r_ms, "it_per_s": 1000.0 / r_ms,
+                                "what": "reference kernels, one view per launch"}
+    return out
+
+
+def run_config_d(dev, flush, rp):
+    """3M 6-D primitives, 4 views of mixed resolution in one launch, tile size
+    picked by the autotuner, peak memory reported."""
+    from ubs import scene as S
+    from ubs.autotune import TileAutotuner
+    p = S.synthetic_params(3_000_000, 6, seed=0, xyz_range=2.0, device=dev)
+    for v in p.values():
+        v.requires_grad_(True)
+    res = [(1920, 1080), (1600, 1064), (1280, 720), (960, 540)]
+    cams = [S.orbit_view(200 + i, 4.0, w, h, 1500.0 * w / 1920, 1500.0 * w / 1920, device=dev)
+            for i, (w, h) in enumerate(res)]
+    tuner = TileAutotuner(reps=3)
+    states = {}
+
+    def tune_step(ts):
+        if ts not in states:
+            states[ts] = TrainViews(p, cams, dev, ts)
+        states[ts].step()
+
+    best = tuner.pick("configD", tune_step)
+    for st in states.values():
+        st.r._check_pending()
+    states.clear()
+    torch.cuda.synchronize()
+    torch.cuda.reset_peak_memory_stats(dev)
+    ms, isects = _train_views(p, cams, dev, best, 10, flush)
+    peak = torch.cuda.max_memory_allocated(dev)
+    out = {"workload": "3M 6-D primitives, views 1920x1080 + 1600x1064 + 1280x720 + 960x540 "
+                       "(fx = 1500 W/1920) in one fused forward + L1 + backward",
+           "tile_size": best, "autotune_ms": {str(k): round(v, 3) for k, v in
+                                              tuner.timings("configD").items()},
+           "ms_per_step": ms, "it_per_s": 1000.0 / ms, "isects": isects,
+           "peak_memory_bytes": int(peak),
+           "peak_memory_note": "torch.cuda.max_memory_allocated over the timed steps "
+                               "(parameters, gradients, workspaces, images)"}
+    if rp is not None:
+        r_ms = _ref_train_views(rp, p, cams, dev, 3, flush)
+        out["ref_gpu_plain"] = {"ms_per_step": r_ms, "it_per_s": 1000.0 / r_ms,
+                                "what": "reference kernels, one view per launch"}
+    return out
+
+
+def run_serving(dev, rp, duration=3.0, rate=200.0):
+    """Resident scenes of 500k, 1M and 3M 6-D primitives; Poisson requests at
+    `rate`/s with resolutions uniform over 640x480, 1280x720, 1920x1080."""
+    from ubs import scene as S
+    from ubs.serve import ServeConfig, Server, latency_stats, poisson_trace, run_plain
+    sizes = {"s500k": 500_000, "s1m": 1_000_000, "s3m": 3_000_000}
+    scenes = {k: S.synthetic_params(n, 6, seed=i, xyz_range=2.0, device=dev)
+              for i, (k, n) in enumerate(sizes.items())}
+    res = [(640, 480), (1280, 720), (1920, 1080)]
+    srv = Server(scenes, ServeConfig(max_slots=4, max_batch_views=8))
+    srv.calibrate({k: S.orbit_view(7, 4.0, 1280, 720, 1000.0, 1000.0, device=dev) for k in scenes})
+    trace = poisson_trace(rate, duration, list(scenes), res, seed=0, device=dev)
+    srv.run(trace[:40], realtime=False)  # warm-up (allocator, kernels)
+    served = latency_stats(srv.run(trace, realtime=True))
+    sat_done = srv.run(trace, realtime=False)
+    saturated = latency_stats(sat_done)
+    out = {"workload": "resident scenes of 500k, 1M, 3M 6-D primitives; Poisson arrivals at "
+                       "%g req/s for %g s (%d requests), resolutions uniform over 640x480, "
+                       "1280x720, 1920x1080, random radius-4 orbit cameras; latency = arrival "
+                       "to image in pinned host memory" % (rate, duration, len(trace)),
+           "served": served, "served_saturated": saturated, "reruns": srv.reruns}
+    bg = torch.zeros(3, device=dev)
+    ri, rj = S.rest_indices(6, dev)
+
+    def dropin_one(r):
+        with torch.no_grad():
+            img, _, _ = S.render_view(scenes[r.scene], r.camera, bg, ri, rj, tile_size=TILE)
+        return img
+
+    run_plain(dropin_one, trace[:20], realtime=False)
+    out["plain_dropin"] = latency_stats(run_plain(dropin_one, trace, realtime=True))
+    out["plain_dropin_saturated"] = latency_stats(run_plain(dropin_one, trace, realtime=False))
+    if rp is not None:
+        def ref_one(r):
+            c = r.camera
+            with torch.no_grad():
+                img, _, _ = rp.render_view(scenes[r.scene], c.viewmat, c.K, c.width, c.height,
+                                           c.center, bg, ri, rj, tile_size=TILE)
+            return img
+
+        run_plain(ref_one, trace[:20], realtime=False)
+        out["plain_ref_gpu"] = latency_stats(run_plain(ref_one, trace, realtime=True))
+        out["plain_ref_gpu_saturated"] = latency_stats(run_plain(ref_one, trace,
+                                                                 realtime=False))
+    return out
 
 
 # ------------------------------------------------------- CPU (oracle port)
@@ -538,6 +711,19 @@ def main():
         except Exception as e:  # noqa: BLE001
             cpu = {"error": str(e)[:200]}
 
+    configs = None
+    if not args.no_configs and rank == 0:
+        rp = _ref_pipeline() if not args.no_ref_gpu else None
+        configs = {}
+        for name, fn in (("C", lambda: run_config_c(dev, flush, rp)),
+                         ("D", lambda: run_config_d(dev, flush, rp)),
+                         ("E", lambda: run_serving(dev, rp))):
+            try:
+                configs[name] = fn()
+            except Exception as e:  # noqa: BLE001
+                configs[name] = {"error": repr(e)[:300]}
+            torch.cuda.empty_cache()
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "it/s", "n_gpus": world,
@@ -566,6 +752,7 @@ def main():
                                     sorted(kernel_ms.items(), key=lambda x: -x[1])},
             "isects": n_isects, "visible": n_visible, "pairs": pairs,
             "wall_s_timed": wall,
+            "configs": configs,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -373,13 +373,18 @@ class RefPipeline:
 
         self.Rot, self.Covar, self.Cond, self.Proj, self.Raster = Rot, Covar, Cond, Proj, Raster
 
-    def render_view(self, p, viewmat, K, W, H, center, background, rest_i, rest_j, tile_size=16):
-        """Same operator sequence as the reference model's render + rasterization()."""
+    def render_view(self, p, viewmat, K, W, H, center, background, rest_i, rest_j, tile_size=16,
+                    timestamp=0.0):
+        """Same operator sequence as the reference model's render + rasterization()
+        (scene/beta_model.py:660-722): 6-D query = view direction, 7-D adds the
+        timestamp."""
         import torch.nn.functional as F
         scale = F.softplus(p["scale"])
         beta = 4.0 * torch.exp(p["beta"])
         view_dir = p["xyz"] - center.unsqueeze(0)
         query = view_dir / view_dir.norm(dim=-1, keepdim=True)
+        if p["scale"].shape[1] == 7:
+            query = torch.cat([query, torch.full_like(query[:, :1], float(timestamp))], -1)
         R = self.Rot.apply(p["l_triangle"][:, :3])
         covar = self.Covar.apply(R, scale, p["l_triangle"], rest_i, rest_j)
         means_nd = torch.cat([p["xyz"], p["mean"]], -1)

@@ -175,6 +175,11 @@ def stream(device=None):
     return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
 
 
+def stream_ptr(s):
+    """cudaStream_t of a torch.cuda.Stream."""
+    return ctypes.c_void_p(s.cuda_stream)
+
+
 def workspace(nbytes, device):
     """Caller-owned scratch memory (the caching allocator aligns to 512 bytes)."""
     return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)

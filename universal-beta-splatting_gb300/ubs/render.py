@@ -30,20 +30,28 @@ STATUS_NEG_DEPTH = 2
 class Views:
     """Cameras of one render call, flattened into (view, tile) buckets and one
     pixel buffer.  `cameras` are ubs.scene.Camera objects (viewmat, K, width,
-    height, timestamp)."""
+    height, timestamp).  The per-view tables go to the device in two copies
+    from one pinned staging buffer, on `stream` (default: the current one)."""
 
-    def __init__(self, cameras: Sequence, tile_size: int = 16, device=None):
+    def __init__(self, cameras: Sequence, tile_size: int = 16, device=None, stream=None):
         if len(cameras) == 0:
             raise ValueError("need at least one view")
         device = torch.device(device or cameras[0].viewmat.device)
         C = len(cameras)
-        vm = torch.stack([c.viewmat.reshape(16).float().cpu() for c in cameras])
-        intr = torch.tensor([[float(c.K[0, 0]), float(c.K[1, 1]), float(c.K[0, 2]),
-                              float(c.K[1, 2])] for c in cameras], dtype=torch.float32)
-        centers = torch.stack([c.center.float().cpu() for c in cameras])
-        times = torch.tensor([float(c.timestamp) for c in cameras], dtype=torch.float32)
+        fl = torch.empty(C * 24, dtype=torch.float32, pin_memory=torch.cuda.is_available())
+        # int64 pix_base [C+1], then int32 dims [C,4] and tile_base [C+1]
+        ints = torch.empty(2 * (C + 1) + 4 * C + C + 1, dtype=torch.int32,
+                           pin_memory=torch.cuda.is_available())
+        f = fl.view(C, 24)
         dims, tile_base, pix_base = [], [0], [0]
-        for c in cameras:
+        for v, c in enumerate(cameras):
+            vm = c.viewmat.detach().reshape(16).float().cpu()
+            f[v, 0:16] = vm
+            K = c.K.detach().float().cpu()
+            f[v, 16:20] = torch.stack([K[0, 0], K[1, 1], K[0, 2], K[1, 2]])
+            R, t = vm.view(4, 4)[:3, :3], vm.view(4, 4)[:3, 3]
+            f[v, 20:23] = -R.t() @ t
+            f[v, 23] = float(c.timestamp)
             tw = (c.width + tile_size - 1) // tile_size
             th = (c.height + tile_size - 1) // tile_size
             dims.append([c.width, c.height, tw, th])
@@ -51,6 +59,10 @@ class Views:
             pix_base.append(pix_base[-1] + c.width * c.height)
         if tile_base[-1] >= 2 ** 31:
             raise ValueError("too many tiles in one render call")
+        o = 2 * (C + 1)
+        ints[:o].view(torch.int64)[:] = torch.tensor(pix_base, dtype=torch.int64)
+        ints[o:o + 4 * C] = torch.tensor(dims, dtype=torch.int32).reshape(-1)
+        ints[o + 4 * C:] = torch.tensor(tile_base, dtype=torch.int32)
         self.C = C
         self.tile_size = tile_size
         self.shapes = [(c.height, c.width) for c in cameras]
@@ -58,13 +70,23 @@ class Views:
         self.n_pixels = pix_base[-1]
         self.pix_base_host = pix_base
         self.device = device
-        self.viewmats = vm.to(device)
-        self.intr = intr.to(device)
-        self.centers = centers.to(device)
-        self.times = times.to(device)
-        self.dims = torch.tensor(dims, dtype=torch.int32).to(device)
-        self.tile_base = torch.tensor(tile_base, dtype=torch.int32).to(device)
-        self.pix_base = torch.tensor(pix_base, dtype=torch.int64).to(device)
+        if device.type == "cuda":
+            st = stream if stream is not None else torch.cuda.current_stream(device)
+            with torch.cuda.stream(st):
+                fd = fl.to(device, non_blocking=True).view(C, 24)
+                idev = ints.to(device, non_blocking=True)
+                self.viewmats = fd[:, 0:16].contiguous()
+                self.intr = fd[:, 16:20].contiguous()
+                self.centers = fd[:, 20:23].contiguous()
+                self.times = fd[:, 23].contiguous()
+        else:  # host-side tables only (no compute runs on them)
+            fd, idev = fl.clone().view(C, 24), ints.clone()
+            self.viewmats, self.intr = fd[:, 0:16].contiguous(), fd[:, 16:20].contiguous()
+            self.centers, self.times = fd[:, 20:23].contiguous(), fd[:, 23].contiguous()
+        self._staging = (fl, ints)  # pinned buffers must outlive the copies
+        self.pix_base = idev[:o].view(torch.int64)
+        self.dims = idev[o:o + 4 * C].view(C, 4)
+        self.tile_base = idev[o + 4 * C:]
 
     def split(self, flat: torch.Tensor) -> List[torch.Tensor]:
         """Per-view [H, W, ...] views of a flat per-pixel buffer."""
