@@ -300,23 +300,38 @@ __global__ void scene_emit_kernel(int64_t CN, int64_t N, const Rec *__restrict__
     }
 }
 
-// Sorted-entry writer of the fused path: the blend's packed record and colour.
-struct RecWriter {
-    const Rec *recs_in;
-    const float *rgb;
-    int64_t N;
-    Rec *recs_out;
-    float4 *cols_out;
+// Sorted-entry writer of the fused path: the sort leaves each sorted key in
+// place; scene_gather_kernel then writes the blend's packed records.
+struct KeyWriter {
+    uint64_t *keys;
     __device__ __forceinline__ void operator()(uint64_t key, int64_t pos, int64_t) const {
-        const int64_t gid = (int64_t)(key & 0xffffffffu);
-        const float4 *src = reinterpret_cast<const float4 *>(recs_in + gid);
-        float4 *dst = reinterpret_cast<float4 *>(recs_out + pos);
-        dst[0] = src[0];
-        dst[1] = src[1];
-        const int64_t n = gid % N;
-        cols_out[pos] = make_float4(rgb[n * 3], rgb[n * 3 + 1], rgb[n * 3 + 2], 0.f);
+        keys[pos] = key;
     }
 };
+
+// One packed record and colour per sorted intersection, gathered by the
+// (view, primitive) index in the key's low word.  A grid-stride loop at full
+// occupancy keeps enough gathers in flight to hide their latency.
+__global__ void __launch_bounds__(256) scene_gather_kernel(const uint64_t *__restrict__ keys,
+                                                           const int64_t *T_dev, int64_t cap,
+                                                           const Rec *__restrict__ recs_in,
+                                                           const float *__restrict__ rgb,
+                                                           int64_t N, Rec *__restrict__ recs_out,
+                                                           float4 *__restrict__ cols_out) {
+    const int64_t T = imin64(*T_dev, cap);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < T; i += stride) {
+        const int64_t gid = (int64_t)(keys[i] & 0xffffffffu);
+        const float4 *src = reinterpret_cast<const float4 *>(recs_in + gid);
+        const float4 a = src[0], b = src[1];
+        const int64_t n = gid % N;
+        const float4 c = make_float4(rgb[n * 3], rgb[n * 3 + 1], rgb[n * 3 + 2], 0.f);
+        float4 *dst = reinterpret_cast<float4 *>(recs_out + i);
+        dst[0] = a;
+        dst[1] = b;
+        cols_out[i] = c;
+    }
+}
 
 template <int D> __global__ void scene_prim_bwd_kernel(SceneArgs a) {
     constexpr int K = D - 3;
@@ -593,10 +608,22 @@ int ubs_scene_forward(int32_t dim, int64_t N, const float *xyz, const float *mea
         note_launch();
         if (int e = check_launch("scene_emit")) return e;
     }
-    const RecWriter wr{w.recs, rgb, N, w.sorted, w.cols};
+    const KeyWriter wr{w.keys};
     if (int e = launch_bucket_sort(n_buckets, w.offsets, &w.hdr->total, capacity, w.keys,
                                    w.scratch, w.big_list, &w.hdr->n_big, wr, st))
         return e;
+    {
+        int dev = 0, sms = 152;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const unsigned grid = (unsigned)imin64(imin64((capacity + 255) / 256, (int64_t)sms * 8),
+                                               (int64_t)1 << 20);
+        UBS_TIMED("scene_gather", st,
+                  scene_gather_kernel<<<grid, 256, 0, st>>>(w.keys, &w.hdr->total, capacity,
+                                                            w.recs, rgb, N, w.sorted, w.cols));
+        note_launch();
+        if (int e = check_launch("scene_gather")) return e;
+    }
     UBS_TIMED("bucket_order", st,
               bucket_order_kernel<<<1, 1024, 0, st>>>(w.offsets, &w.hdr->total, capacity,
                                                       n_buckets, w.order));
