@@ -60,8 +60,10 @@ def parse():
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the batched (C, D) and serving (E) configurations")
     ap.add_argument("--profile", action="store_true",
-                    help="run only the fused step (first frame, --warmup steps, one more step) "
+                    help="run only the fused step (capture, --warmup replays and one more) "
                          "for an ncu capture; prints no JSON line")
+    ap.add_argument("--eager", action="store_true",
+                    help="with --profile: launch the step kernel by kernel instead of a graph")
     return ap.parse_args()
 
 
@@ -188,8 +190,9 @@ class FusedStep:
             self.renderer.render(self.p, self.views, self.bg, check=False)
 
 
-def time_steps(fn, K, dev, flush):
-    """Per-step CUDA-event time (ms), L2 flushed before every step (untimed)."""
+def time_steps(fn, K, dev, flush, after=None):
+    """Per-step CUDA-event time (ms), L2 flushed before every step (untimed);
+    `after` runs after each step, outside the timed events."""
     total = 0.0
     for k in range(K):
         flush.fill_(float(k))
@@ -200,6 +203,8 @@ def time_steps(fn, K, dev, flush):
         e1.record()
         e1.synchronize()
         total += e0.elapsed_time(e1)
+        if after is not None:
+            after()
     return total / K
 
 
@@ -569,7 +574,7 @@ def main():
     L.lib()
     p, cam, ri, rj, bg, target = make_problem(args.n_prims, rank, dev)
     fz = FusedStep(p, cam, bg, target, dev)
-    if args.profile:
+    if args.profile and args.eager:
         fz.prime()
         for _ in range(args.warmup + 1):
             fz.step()
@@ -577,27 +582,41 @@ def main():
         fz.renderer._check_pending()
         print("profile run: %d intersections" % fz.renderer.last_isects, flush=True)
         return
+    from ubs.render import GraphedStep, Renderer
+    g_target = fz.target.clone()
+    g_ren = Renderer(dim=DIM, tile_size=TILE)
+    prof_slots = 64 * 4
+    gs = GraphedStep(g_ren, p, fz.views, fz.bg,
+                     lambda colors, alphas: (colors - g_target).abs().mean(),
+                     before_capture=lambda: L.profile_start(prof_slots))
+    if args.profile:
+        L.profile_stop()
+        for _ in range(args.warmup + 1):
+            gs.replay()
+        torch.cuda.synchronize()
+        gs.check()
+        print("profile run (graph): %d intersections" % g_ren.last_isects, flush=True)
+        return
     flush = l2_flush_buffer(dev)
     clocks = ClockSampler()
     clocks.start()
-    fz.prime()
     for _ in range(max(3, args.warmup)):
-        fz.step()
+        gs.replay()
     torch.cuda.synchronize()
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
     torch.cuda.synchronize()
-    launches0 = L.query("ubs_launch_count")
     clocks.mark("t0")
     t_wall = time.perf_counter()
-    L.profile_start(64 * (args.steps + 1))
-    ms = time_steps(fz.step, args.steps, dev, flush)
+    ms = time_steps(gs.replay, args.steps, dev, flush, after=L.profile_sample)
     kernels = L.profile_stop()
     wall = time.perf_counter() - t_wall
     clocks.mark("t1")
-    fz.renderer._check_pending()  # raises if any timed frame overflowed its buffers
-    launches = L.query("ubs_launch_count") - launches0
+    gs.check()  # raises if the replayed frame overflowed its buffers
+    # kernel launches of this library inside the timed region: the graph's
+    # library kernels, once per replay (the host-side counter sees the capture)
+    launches = gs.launches_per_replay * args.steps
     torch.cuda.synchronize()
     ms_max = ms
     if world > 1:
@@ -610,9 +629,9 @@ def main():
     kernel_ms = {k: t / args.steps for k, (n, t) in kernels.items()}
 
     # end to end through the public API: parameters and target copied from
-    # pinned host memory every step, the loss read back
+    # pinned host memory into the step's tensors every step, the loss read back
     host = {k: v.detach().cpu().pin_memory() for k, v in p.items()}
-    host_target = fz.target.cpu().pin_memory()
+    host_target = g_target.cpu().pin_memory()
     h2d = sum(v.numel() * 4 for v in host.values()) + host_target.numel() * 4
     loss_host = torch.empty(1, pin_memory=True)
 
@@ -620,16 +639,22 @@ def main():
         with torch.no_grad():
             for k, v in p.items():
                 v.copy_(host[k], non_blocking=True)
-            fz.target.copy_(host_target, non_blocking=True)
-        loss = fz.step()
+            g_target.copy_(host_target, non_blocking=True)
+        loss = gs.replay()
         loss_host.copy_(loss.detach().view(1), non_blocking=True)
 
     for _ in range(2):
         e2e_step()
     e2e_ms = time_steps(e2e_step, args.steps, dev, flush)
-    fz.renderer._check_pending()
+    gs.check()
     e2e_val = world * 1000.0 / e2e_ms
     clocks.stop()
+    # the same step without the graph (one launch per kernel from the host)
+    fz.prime()
+    for _ in range(3):
+        fz.step()
+    eager_ms = time_steps(fz.step, max(20, min(args.steps, 100)), dev, flush)
+    fz.renderer._check_pending()
     fwd_ms = time_steps(fz.forward, max(5, min(args.steps, 20)), dev, flush)
     fz.renderer._check_pending()
 
@@ -667,7 +692,8 @@ def main():
         "peak_source": "measured: FP32 FMA probe kernel timed in this run (MEASURED_PEAKS.json "
                        "has HBM %s GB/s and bf16 only)" % peaks.get("hbm_gbs", "n/a"),
         "launch_ms": dom_ms,
-        "timing": "CUDA events on the launching stream around each launch, timed region",
+        "timing": "CUDA events on the launching stream around each launch (graph event "
+                  "nodes), every replay of the timed region",
     }
 
     # the reference's own kernels, plain one-view-per-launch path, same GPU
@@ -735,7 +761,8 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "256 MB buffer written before every timed step (untimed); "
                              "per-step CUDA events",
-                       "path": "fused scene render (ubs.render.Renderer)"},
+                       "path": "fused scene render (ubs.render.Renderer), whole step "
+                               "replayed as one CUDA graph (ubs.render.GraphedStep)"},
             "render_fps": 1000.0 / fwd_ms,
             "e2e": {"value": e2e_val, "unit": "it/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": 4},
@@ -744,6 +771,8 @@ def main():
             "roofline": roofline,
             "cpu_baseline": cpu,
             "ref_gpu": ref_gpu,
+            "eager": {"value": 1000.0 / eager_ms, "unit": "it/s", "ms_per_step": eager_ms,
+                      "what": "the same fused step launched kernel by kernel (no graph)"},
             "dropin": {"value": 1000.0 / d_ms, "unit": "it/s", "ms_per_step": d_ms,
                        "render_fps": 1000.0 / d_fwd_ms,
                        "what": "the same step through the drop-in gsplat operators"},

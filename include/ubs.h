@@ -48,8 +48,13 @@ unsigned long long ubs_launch_count(void);
  * pool of max_launches pairs created by start (launches beyond the pool are
  * not timed).  stop waits for the recorded events and aggregates the
  * durations per kernel name; ubs_profile_result(i, ...) reads entry i < n.
- * Start and stop are host-side set-up: call them outside stream capture. */
+ * Start and stop are host-side set-up: call them outside stream capture.
+ * Launches captured into a CUDA graph while timing is on get their event pair
+ * as external event-record nodes, recorded again by every replay: call
+ * ubs_profile_sample after each replay (it waits for the events and adds the
+ * durations); stop then aggregates the samples instead of taking one. */
 int ubs_profile_start(int32_t max_launches);
+int ubs_profile_sample(void);
 int ubs_profile_stop(int32_t *n_kernels);
 int ubs_profile_result(int32_t i, const char **name, int64_t *launches, double *total_ms);
 /* FP32 FMA issue-rate probe (no reference counterpart): 8 CTAs of 256 threads

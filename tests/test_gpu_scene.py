@@ -119,3 +119,34 @@ def test_fused_unchecked_overflow_is_reported():
         colors, _ = r.render(p, views, check=True)
     img_d, _, _ = dropin_render(p, cam, torch.zeros(3, device=DEV))
     assert float((views.split(colors)[0] - img_d).abs().max()) < 1e-5
+
+
+def test_graphed_step_matches_eager_and_follows_parameter_updates():
+    from ubs.render import GraphedStep
+    p = make_params(6000, 6, seed=31)
+    cam = S.orbit_view(9, 3.0, 320, 240, 280.0, 280.0, device=DEV)
+    g = torch.Generator().manual_seed(8)
+    target = torch.rand(240 * 320, 3, generator=g).to(DEV)
+    leaves = {k: v.clone().requires_grad_(True) for k, v in p.items()}
+    views = Views([cam], device=DEV)
+    loss_fn = lambda colors, alphas: (colors - target).abs().mean()  # noqa: E731
+    gs = GraphedStep(Renderer(dim=6), leaves, views, None, loss_fn)
+    assert gs.launches_per_replay >= 8
+
+    def eager():
+        ref = {k: v.detach().clone().requires_grad_(True) for k, v in leaves.items()}
+        colors, alphas = Renderer(dim=6).render(ref, Views([cam], device=DEV))
+        loss = loss_fn(colors, alphas)
+        loss.backward()
+        return float(loss), {k: v.grad for k, v in ref.items()}
+
+    for step in range(3):
+        loss = float(gs.replay())
+        gs.check()
+        l_ref, g_ref = eager()
+        assert abs(loss - l_ref) <= 1e-6 * abs(l_ref)
+        for k in g_ref:
+            assert rel_l2(leaves[k].grad, g_ref[k]) < 1e-5, (step, k)
+        with torch.no_grad():  # an in-place parameter update, as an optimizer makes
+            for v in leaves.values():
+                v.add_(0.01 * torch.randn_like(v))

@@ -51,6 +51,8 @@ namespace {
 struct ProfSlot {
     const char *name;
     cudaEvent_t e0, e1;
+    double acc_ms;   // accumulated by samples
+    long long n;     // samples taken
 };
 struct ProfEntry {
     const char *name;
@@ -64,17 +66,42 @@ std::atomic<bool> g_prof_on{false};
 std::atomic<int> g_prof_next{0};
 } // namespace
 
+// Inside stream capture the events become external event-record nodes of
+// the graph, so every replay records them again (read with ubs_profile_sample).
+static cudaError_t prof_record(cudaEvent_t e, cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) return cudaErrorUnknown;
+    return cudaEventRecordWithFlags(
+        e, st, cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault);
+}
+
 KernelTimer::KernelTimer(const char *name, cudaStream_t s) : slot(-1), st(s) {
     if (!g_prof_on.load(std::memory_order_acquire)) return;
     const int i = g_prof_next.fetch_add(1, std::memory_order_relaxed);
     if (i >= (int)g_prof_slots.size()) return; // pool exhausted: launch is not timed
     g_prof_slots[i].name = name;
-    if (cudaEventRecord(g_prof_slots[i].e0, st) == cudaSuccess) slot = i;
+    if (prof_record(g_prof_slots[i].e0, st) == cudaSuccess) slot = i;
 }
 
 KernelTimer::~KernelTimer() {
-    if (slot >= 0 && cudaEventRecord(g_prof_slots[slot].e1, st) != cudaSuccess)
+    if (slot >= 0 && prof_record(g_prof_slots[slot].e1, st) != cudaSuccess)
         g_prof_slots[slot].name = nullptr;
+}
+
+// Adds the current duration of every recorded event pair to its slot.
+static int prof_sample_locked() {
+    const int n = std::min<int>(g_prof_next.load(), (int)g_prof_slots.size());
+    for (int i = 0; i < n; ++i) {
+        ProfSlot &p = g_prof_slots[i];
+        if (!p.name) continue;
+        float ms = 0.f;
+        if (cudaEventSynchronize(p.e1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, p.e0, p.e1) != cudaSuccess)
+            return check_launch("profile sample");
+        p.acc_ms += ms;
+        p.n += 1;
+    }
+    return UBS_OK;
 }
 
 static void prof_release() {
@@ -131,16 +158,29 @@ int ubs_profile_start(int32_t max_launches) {
         g_prof_slots.resize(max_launches);
         for (auto &p : g_prof_slots) {
             p.name = nullptr;
+            p.acc_ms = 0.0;
+            p.n = 0;
             if (cudaEventCreate(&p.e0) != cudaSuccess || cudaEventCreate(&p.e1) != cudaSuccess) {
                 g_prof_slots.clear();
                 return check_launch("profile_start event pool");
             }
         }
     }
+    for (auto &p : g_prof_slots) {
+        p.name = nullptr;
+        p.acc_ms = 0.0;
+        p.n = 0;
+    }
     g_prof_result.clear();
     g_prof_next.store(0);
     g_prof_on.store(true, std::memory_order_release);
     return UBS_OK;
+}
+
+int ubs_profile_sample(void) {
+    using namespace ubs;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    return prof_sample_locked();
 }
 
 int ubs_profile_stop(int32_t *n_kernels) {
@@ -149,13 +189,13 @@ int ubs_profile_stop(int32_t *n_kernels) {
     if (!g_prof_on.load()) return set_error(UBS_ERR_INVALID, "profile_stop: not running");
     g_prof_on.store(false, std::memory_order_release);
     const int n = std::min<int>(g_prof_next.load(), (int)g_prof_slots.size());
+    bool sampled = false;
+    for (int i = 0; i < n; ++i) sampled = sampled || g_prof_slots[i].n > 0;
+    if (!sampled)
+        if (int e = prof_sample_locked()) return e;
     for (int i = 0; i < n; ++i) {
         const ProfSlot &p = g_prof_slots[i];
-        if (!p.name) continue;
-        float ms = 0.f;
-        if (cudaEventSynchronize(p.e1) != cudaSuccess ||
-            cudaEventElapsedTime(&ms, p.e0, p.e1) != cudaSuccess)
-            return check_launch("profile_stop");
+        if (!p.name || p.n == 0) continue;
         ProfEntry *e = nullptr;
         for (auto &r : g_prof_result)
             if (std::strcmp(r.name, p.name) == 0) e = &r;
@@ -163,8 +203,8 @@ int ubs_profile_stop(int32_t *n_kernels) {
             g_prof_result.push_back({p.name, 0, 0.0});
             e = &g_prof_result.back();
         }
-        e->launches += 1;
-        e->ms += ms;
+        e->launches += p.n;
+        e->ms += p.acc_ms;
     }
     if (n_kernels) *n_kernels = (int32_t)g_prof_result.size();
     return UBS_OK;

@@ -279,24 +279,34 @@ __device__ __forceinline__ void blend_pair(const GeoRec &q, const float (&col)[C
     const bool v0 = !d0 && !(s0 < 0.f || s0 >= 1.f);
     const bool v1 = !d1 && !(s1 < 0.f || s1 >= 1.f);
     if (!__any_sync(0xffffffffu, v0 || v1)) return;
-    const float a0 = fminf(0.999f, q.opac * __powf(v0 ? 1.f - s0 : 1.f, q.beta));
-    const float a1 = fminf(0.999f, q.opac * __powf(v1 ? 1.f - s1 : 1.f, q.beta));
-    const float n0 = T0 * (1.f - a0), n1 = T1 * (1.f - a1);
-    const bool t0 = v0 && n0 <= 1e-4f, t1 = v1 && n1 <= 1e-4f;
-    const bool b0 = v0 && !t0, b1 = v1 && !t1;
-    d0 = d0 || t0;
-    d1 = d1 || t1;
-    const float w0 = b0 ? a0 * T0 : 0.f, w1 = b1 ? a1 * T1 : 0.f;
+    if (v0) {
+        const float a0 = fminf(0.999f, q.opac * __powf(1.f - s0, q.beta));
+        const float n0 = T0 * (1.f - a0);
+        if (n0 <= 1e-4f) {
+            d0 = true;
+        } else {
+            const float w0 = a0 * T0;
 #pragma unroll
-    for (int k = 0; k < CD; ++k) {
-        acc0[k] += col[k] * w0;
-        acc1[k] += col[k] * w1;
+            for (int k = 0; k < CD; ++k) acc0[k] += col[k] * w0;
+            T0 = n0;
+            cur0 = idx;
+            if (COUNT) ++n_contrib;
+        }
     }
-    T0 = b0 ? n0 : T0;
-    T1 = b1 ? n1 : T1;
-    cur0 = b0 ? idx : cur0;
-    cur1 = b1 ? idx : cur1;
-    if (COUNT) n_contrib += (uint32_t)b0 + (uint32_t)b1;
+    if (v1) {
+        const float a1 = fminf(0.999f, q.opac * __powf(1.f - s1, q.beta));
+        const float n1 = T1 * (1.f - a1);
+        if (n1 <= 1e-4f) {
+            d1 = true;
+        } else {
+            const float w1 = a1 * T1;
+#pragma unroll
+            for (int k = 0; k < CD; ++k) acc1[k] += col[k] * w1;
+            T1 = n1;
+            cur1 = idx;
+            if (COUNT) ++n_contrib;
+        }
+    }
 }
 
 // --------------------------------------------------------------- forward

@@ -65,6 +65,7 @@ SIGNATURES = {
     "ubs_scene_stats": ([_P, _I64P, _U32P, _P], _INT),
     "ubs_profile_start": ([_I32], _INT),
     "ubs_profile_stop": ([ctypes.POINTER(_I32)], _INT),
+    "ubs_profile_sample": ([], _INT),
     "ubs_profile_result": ([_I32, ctypes.POINTER(ctypes.c_char_p), _I64P,
                             ctypes.POINTER(ctypes.c_double)], _INT),
     "ubs_fp32_probe_workspace_bytes": ([], _SZ),
@@ -140,6 +141,11 @@ def profile_start(max_launches=4096):
     """Time every kernel the library launches from now on (CUDA events on the
     launching stream)."""
     call("ubs_profile_start", int(max_launches))
+
+
+def profile_sample():
+    """After a CUDA-graph replay: add the replay's kernel durations."""
+    call("ubs_profile_sample")
 
 
 def profile_stop():

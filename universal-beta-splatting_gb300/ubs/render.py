@@ -118,6 +118,7 @@ class Renderer:
         self.exact_cond_grad = exact_cond_grad
         self.last_isects = None
         self._pending = None  # (pinned stats, event, capacity) of an unchecked frame
+        self.last_ws, self.last_cap = None, None
 
     # ---------------------------------------------------------------- helpers
     def _check_pending(self):
@@ -135,6 +136,22 @@ class Renderer:
             raise RuntimeError("scene render: an earlier unchecked frame needed %d intersections "
                                "but had capacity %d; capacity is now %d" % (T, cap, self.capacity))
 
+    def stats(self):
+        """(intersections, status bits) of the last forward's workspace; raises
+        if that frame overflowed its capacity.  Synchronises the stream."""
+        import ctypes
+        T, status = ctypes.c_int64(0), ctypes.c_uint32(0)
+        L.call("ubs_scene_stats", L.ptr(self.last_ws), ctypes.byref(T), ctypes.byref(status),
+               L.stream(self.last_ws.device))
+        self.last_isects = int(T.value)
+        if status.value & STATUS_NEG_DEPTH:
+            raise RuntimeError("scene render: a visible primitive has a negative depth")
+        if status.value & STATUS_OVERFLOW or T.value > self.last_cap:
+            self.capacity = max(self.capacity or 0, int(T.value * 1.25) + 1024)
+            raise RuntimeError("scene render: a frame needed %d intersections but had capacity "
+                               "%d; capacity is now %d" % (T.value, self.last_cap, self.capacity))
+        return int(T.value), int(status.value)
+
     def workspace_bytes(self, C, N, n_buckets, capacity):
         return L.query("ubs_scene_workspace_bytes", C, N, n_buckets, capacity)
 
@@ -146,8 +163,18 @@ class Renderer:
             float(self.radius_clip), L.ptr(bg)]
 
     def forward_raw(self, p: Dict[str, torch.Tensor], views: Views, bg, check=True):
-        """Run the forward kernels; returns (colors, alphas, last_ids, workspace, capacity)."""
-        self._check_pending()
+        """Run the forward kernels; returns (colors, alphas, last_ids, workspace, capacity).
+
+        check=True reads the intersection count back (synchronising) and
+        re-runs an overflowing frame; check=False reads it back
+        asynchronously and reports an overflow at the next call; check="none"
+        issues nothing but the kernels (safe inside CUDA graph capture) and
+        leaves the verification to `stats()` after the frame(s)."""
+        if check == "none":
+            if self.capacity is None:
+                raise RuntimeError("check='none' needs a capacity (render once with check=True)")
+        else:
+            self._check_pending()
         N = p["xyz"].shape[0]
         dev = p["xyz"].device
         cap = self.capacity or max(1 << 16, 16 * N * views.C)
@@ -159,6 +186,9 @@ class Renderer:
             st = L.stream(dev)
             L.call("ubs_scene_forward", *self._args(p, views, bg), L.ptr(colors), L.ptr(alphas),
                    L.ptr(last), cap, L.ptr(ws), ws.numel(), st)
+            self.last_ws, self.last_cap = ws, cap
+            if check == "none":
+                return colors, alphas, last, ws, cap
             stats = torch.empty(2, dtype=torch.int64, pin_memory=True)
             hdr = ws[:16].view(torch.int64)
             if check:
@@ -181,8 +211,9 @@ class Renderer:
             return colors, alphas, last, ws, cap
 
     def render(self, params: Dict[str, torch.Tensor], views: Views,
-               backgrounds: Optional[torch.Tensor] = None, check: bool = True):
-        """Differentiable render of all views: colors [P, 3], alphas [P]."""
+               backgrounds: Optional[torch.Tensor] = None, check=True):
+        """Differentiable render of all views: colors [P, 3], alphas [P].
+        `check`: True, False or "none", as for forward_raw."""
         dev = params["xyz"].device
         if backgrounds is None:
             bg = torch.zeros(views.C, 3, device=dev)
@@ -231,3 +262,59 @@ class _SceneRender(torch.autograd.Function):
         ctx.ws = None
         return (None, None, None, None, g["xyz"], g["mean"], g["scale"], g["l_triangle"],
                 g["opacity"].view(ctx.opacity_shape), g["beta"], g["rgb"])
+
+
+class GraphedStep:
+    """One training step -- fused render of `views`, `loss_fn(colors, alphas)`,
+    backward to every parameter -- captured once into a CUDA graph and then
+    replayed with a single launch.
+
+    The parameters must keep their storage between replays (update them in
+    place, e.g. with an optimizer or `copy_`); after each replay their `.grad`
+    tensors (owned by the graph's memory pool) hold that step's gradients and
+    `loss` holds its value.  The intersection capacity is fixed when the step
+    is captured (the first frame's count times `headroom`); `check()` reads the
+    last replay's count back and raises if the frame overflowed, in which case
+    the step must be captured again."""
+
+    def __init__(self, renderer: Renderer, params: Dict[str, torch.Tensor], views: Views,
+                 backgrounds: Optional[torch.Tensor], loss_fn, headroom: float = 1.5,
+                 warmup: int = 3, before_capture=None):
+        self.r, self.p, self.views, self.loss_fn = renderer, params, views, loss_fn
+        dev = params["xyz"].device
+        self.bg = (torch.zeros(views.C, 3, device=dev) if backgrounds is None
+                   else backgrounds.reshape(-1, 3).expand(views.C, 3).contiguous().float())
+        with torch.no_grad():
+            renderer.render(params, views, self.bg, check=True)
+        renderer.capacity = int(renderer.last_isects * headroom) + 4096
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            for _ in range(warmup):
+                for v in params.values():
+                    v.grad = None
+                self._body()
+        torch.cuda.current_stream(dev).wait_stream(side)
+        for v in params.values():
+            v.grad = None
+        if before_capture is not None:
+            before_capture()
+        self.graph = torch.cuda.CUDAGraph()
+        n0 = L.query("ubs_launch_count")
+        with torch.cuda.graph(self.graph):
+            self.loss = self._body()
+        # library kernels in the graph (each replay launches them all)
+        self.launches_per_replay = int(L.query("ubs_launch_count") - n0)
+
+    def _body(self):
+        colors, alphas = self.r.render(self.p, self.views, self.bg, check="none")
+        loss = self.loss_fn(colors, alphas)
+        loss.backward()
+        return loss
+
+    def replay(self):
+        self.graph.replay()
+        return self.loss
+
+    def check(self):
+        return self.r.stats()
