@@ -177,7 +177,8 @@ class Renderer:
             self._check_pending()
         N = p["xyz"].shape[0]
         dev = p["xyz"].device
-        cap = self.capacity or max(1 << 16, 16 * N * views.C)
+        # first frame: a guess from the pixel count (re-run below if too small)
+        cap = self.capacity or max(1 << 16, min(16 * N * views.C, 8 * views.n_pixels))
         while True:
             ws = L.workspace(self.workspace_bytes(views.C, N, views.n_buckets, cap), dev)
             colors = torch.empty(views.n_pixels, 3, device=dev)
