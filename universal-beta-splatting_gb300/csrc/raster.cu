@@ -262,51 +262,50 @@ __device__ __forceinline__ void load_color(const float4 *scol4, const float *sco
 // One front-to-back blend step of a thread's two pixels (column px, rows py0
 // and py0 + 1) over record q (rasterize_to_pixels_fwd.cu:139-171): skip when
 // sigma is outside [0, 1), alpha = min(0.999, opacity (1 - sigma)^beta), stop
-// (exclusively) once the transmittance would reach 1e-4.  sigma is written as
-// the reference writes it, so the shared products of the two pixels are formed
-// once; the rest is select-based so that a warp issues it once for both pixels
-// and all lanes.  Lanes whose record is skipped evaluate finite dummies that
-// the selects discard.
+// (exclusively) once the transmittance would reach 1e-4.  The pixel pair is
+// evaluated two-wide with Blackwell's packed FP32x2 instructions (__ffma2_rn,
+// __fadd2_rn, __fmul2_rn: per component the same rounding as the scalar
+// operations); (1 - sigma)^beta is formed as 2^(beta log2(1 - sigma)).  The
+// updates are select-based so that a warp issues them once for both pixels
+// and all lanes; lanes whose record is skipped evaluate dummies that the
+// selects discard.
 template <int CD, bool COUNT>
 __device__ __forceinline__ void blend_pair(const GeoRec &q, const float (&col)[CD], float px,
-                                           float py0, float py1, float &T0, float &T1,
-                                           float (&acc0)[CD], float (&acc1)[CD], int32_t &cur0,
-                                           int32_t &cur1, bool &d0, bool &d1, int32_t idx,
-                                           uint32_t &n_contrib) {
-    const float dx = q.x - px, dy0 = q.y - py0, dy1 = q.y - py1;
-    const float s0 = (q.cxx * dx * dx + q.cyy * dy0 * dy0) + 2.f * q.cxy * dx * dy0;
-    const float s1 = (q.cxx * dx * dx + q.cyy * dy1 * dy1) + 2.f * q.cxy * dx * dy1;
-    const bool v0 = !d0 && !(s0 < 0.f || s0 >= 1.f);
-    const bool v1 = !d1 && !(s1 < 0.f || s1 >= 1.f);
+                                           float2 npy, float2 &T, float2 (&acc)[CD],
+                                           int32_t &cur0, int32_t &cur1, bool &d0, bool &d1,
+                                           int32_t idx, uint32_t &n_contrib) {
+    const float dx = q.x - px;
+    const float2 dy = __fadd2_rn(make_float2(q.y, q.y), npy);
+    const float A = q.cxx * dx * dx;
+    const float B = 2.f * q.cxy * dx;
+    float2 s = __fmul2_rn(make_float2(q.cyy, q.cyy), dy);
+    s = __ffma2_rn(s, dy, make_float2(A, A));
+    s = __ffma2_rn(make_float2(B, B), dy, s);
+    const bool v0 = !d0 && !(s.x < 0.f || s.x >= 1.f);
+    const bool v1 = !d1 && !(s.y < 0.f || s.y >= 1.f);
     if (!__any_sync(0xffffffffu, v0 || v1)) return;
-    if (v0) {
-        const float a0 = fminf(0.999f, q.opac * __powf(1.f - s0, q.beta));
-        const float n0 = T0 * (1.f - a0);
-        if (n0 <= 1e-4f) {
-            d0 = true;
-        } else {
-            const float w0 = a0 * T0;
+    const float2 om = __ffma2_rn(s, make_float2(-1.f, -1.f), make_float2(1.f, 1.f));
+    const float2 l = make_float2(__log2f(om.x), __log2f(om.y));
+    const float2 e = __fmul2_rn(l, make_float2(q.beta, q.beta));
+    const float2 p = make_float2(exp2f(e.x), exp2f(e.y));
+    float2 a = __fmul2_rn(make_float2(q.opac, q.opac), p);
+    a.x = fminf(0.999f, a.x);
+    a.y = fminf(0.999f, a.y);
+    const float2 n = __fmul2_rn(T, __ffma2_rn(a, make_float2(-1.f, -1.f), make_float2(1.f, 1.f)));
+    const bool t0 = v0 && n.x <= 1e-4f, t1 = v1 && n.y <= 1e-4f;
+    const bool b0 = v0 && !t0, b1 = v1 && !t1;
+    d0 = d0 || t0;
+    d1 = d1 || t1;
+    float2 w = __fmul2_rn(a, T);
+    w.x = b0 ? w.x : 0.f;
+    w.y = b1 ? w.y : 0.f;
 #pragma unroll
-            for (int k = 0; k < CD; ++k) acc0[k] += col[k] * w0;
-            T0 = n0;
-            cur0 = idx;
-            if (COUNT) ++n_contrib;
-        }
-    }
-    if (v1) {
-        const float a1 = fminf(0.999f, q.opac * __powf(1.f - s1, q.beta));
-        const float n1 = T1 * (1.f - a1);
-        if (n1 <= 1e-4f) {
-            d1 = true;
-        } else {
-            const float w1 = a1 * T1;
-#pragma unroll
-            for (int k = 0; k < CD; ++k) acc1[k] += col[k] * w1;
-            T1 = n1;
-            cur1 = idx;
-            if (COUNT) ++n_contrib;
-        }
-    }
+    for (int k = 0; k < CD; ++k) acc[k] = __ffma2_rn(make_float2(col[k], col[k]), w, acc[k]);
+    T.x = b0 ? n.x : T.x;
+    T.y = b1 ? n.y : T.y;
+    cur0 = b0 ? idx : cur0;
+    cur1 = b1 ? idx : cur1;
+    if (COUNT) n_contrib += (uint32_t)b0 + (uint32_t)b1;
 }
 
 // --------------------------------------------------------------- forward
@@ -354,12 +353,13 @@ __global__ void __launch_bounds__(512) raster_fwd_kernel(RasterArgs a) {
     const int nb = (re - rs + BR - 1) / BR;
 
     const float px = (float)j + 0.5f, py0 = (float)i0 + 0.5f, py1 = py0 + 1.f;
-    float T0 = 1.0f, T1 = 1.0f;
+    const float2 npy = make_float2(-py0, -py1);
+    float2 T = make_float2(1.0f, 1.0f);
     int32_t cur0 = 0, cur1 = 0;
     uint32_t n_contrib = 0;
-    float acc0[CD], acc1[CD];
+    float2 acc[CD];
 #pragma unroll
-    for (int k = 0; k < CD; ++k) acc0[k] = acc1[k] = 0.f;
+    for (int k = 0; k < CD; ++k) acc[k] = make_float2(0.f, 0.f);
     bool d0 = !in0, d1 = !in1;
 
     if (nb > 0) {
@@ -415,8 +415,8 @@ __global__ void __launch_bounds__(512) raster_fwd_kernel(RasterArgs a) {
                         const GeoRec q = batch[t];
                         float col[CD];
                         load_color<CD, PACK>(scol4, scol, buf * BR + t, col);
-                        blend_pair<CD, COUNT>(q, col, px, py0, py1, T0, T1, acc0, acc1, cur0,
-                                              cur1, d0, d1, bs + t, n_contrib);
+                        blend_pair<CD, COUNT>(q, col, px, npy, T, acc, cur0, cur1, d0, d1,
+                                              bs + t, n_contrib);
                         if (__all_sync(0xffffffffu, d0 && d1)) {
                             warp_done = true;
                             break;
@@ -438,15 +438,15 @@ __global__ void __launch_bounds__(512) raster_fwd_kernel(RasterArgs a) {
         if (lane == 0 && w) atomicAdd(a.pair_count, (unsigned long long)w);
     }
     if (in0) {
-        a.out_a[pix0] = 1.0f - T0;
+        a.out_a[pix0] = 1.0f - T.x;
 #pragma unroll
-        for (int k = 0; k < CD; ++k) a.out_c[pix0 * CD + k] = bg ? acc0[k] + T0 * bg[k] : acc0[k];
+        for (int k = 0; k < CD; ++k) a.out_c[pix0 * CD + k] = bg ? acc[k].x + T.x * bg[k] : acc[k].x;
         a.last_ids[pix0] = cur0;
     }
     if (in1) {
-        a.out_a[pix1] = 1.0f - T1;
+        a.out_a[pix1] = 1.0f - T.y;
 #pragma unroll
-        for (int k = 0; k < CD; ++k) a.out_c[pix1 * CD + k] = bg ? acc1[k] + T1 * bg[k] : acc1[k];
+        for (int k = 0; k < CD; ++k) a.out_c[pix1 * CD + k] = bg ? acc[k].y + T.y * bg[k] : acc[k].y;
         a.last_ids[pix1] = cur1;
     }
 }
@@ -481,69 +481,85 @@ __device__ __forceinline__ void bwd_pix_init(BwdPix<CD> &s, const RasterArgs &a,
     s.S = 0.f;
 }
 
-// One back-to-front step of one pixel (rasterize_to_pixels_bwd.cu:158-247),
-// select-based: `valid` lanes (inside, at or before their last contributor,
-// sigma in [0, 1)) add their contributions to
-//   g = [w (cxx dx + cxy dy), w (cxy dx + cyy dy), w dx^2, w dx dy, w dy^2,
-//        vis v_alpha, vis v_alpha log2(1 - sigma), fac v_colour (CD)]
-// with w = v_alpha (1 - sigma)^(beta - 1); the record's constant factors
-// (-2 opacity beta, -opacity beta, opacity ln 2) are applied once after the
-// warp reduction (record_scales).  Other lanes evaluate finite dummies
-// (1 - sigma replaced by 1) whose contributions the selects zero.
-template <int CD>
-__device__ __forceinline__ void grad_px(const GeoRec &q, const float (&col)[CD], float dx,
-                                        float dy, float sigma, bool valid, BwdPix<CD> &s,
-                                        float (&g)[7 + CD]) {
-    const float om = valid ? 1.f - sigma : 1.f;
-    const float vis = __powf(om, q.beta);
-    const float alpha = fminf(0.999f, q.opac * vis);
-    const float ra = 1.0f / (1.0f - alpha);
-    const float Tn = s.T * ra;
-    const float fac = valid ? alpha * Tn : 0.f;
-    float cv = 0.f;
-#pragma unroll
-    for (int k = 0; k < CD; ++k) {
-        g[7 + k] += fac * s.vrc[k];
-        cv += col[k] * s.vrc[k];
-    }
-    const float v_alpha = (valid && q.opac * vis <= 0.999f) ? Tn * cv + ra * (s.K - s.S) : 0.f;
-    const float w = v_alpha * __fdividef(vis, om);
-    g[0] += w * (q.cxx * dx + q.cxy * dy);
-    g[1] += w * (q.cxy * dx + q.cyy * dy);
-    g[2] += w * (dx * dx);
-    g[3] += w * (dx * dy);
-    g[4] += w * (dy * dy);
-    const float u = vis * v_alpha;
-    g[5] += u;
-    g[6] += u * __log2f(om);
-    s.S += fac * cv;
-    s.T = valid ? Tn : s.T;
-}
-
-// Both pixels of a thread against record q; returns whether any lane of the
-// warp had a valid pixel (and so whether g needs reducing).
+// One back-to-front step of both pixels of a thread against record q
+// (rasterize_to_pixels_bwd.cu:158-247: transmittance recovered as
+// T / (1 - alpha), v_alpha from the colour behind and the final alpha, the
+// sigma chain when opacity (1 - sigma)^beta <= 0.999), packed two-wide (one
+// FP32x2 instruction per step for the pixel pair); valid lanes are inside,
+// at or before their last contributor, with sigma in [0, 1), others evaluate
+// finite dummies (1 - sigma replaced by 1) that selects zero.  Returns
+// whether any lane of the warp had a valid pixel.  g receives the pair's sums
+//   [w dx, w dy, w dx^2, w dx dy, w dy^2, vis v_alpha, vis v_alpha log2(1-s),
+//    fac v_colour (CD)],  w = v_alpha (1 - sigma)^(beta - 1),
+// turned into [v_xy, v_conic, v_opacity, v_beta, v_colour] per record at
+// the flush (the conic, -opacity beta and opacity ln 2 factors).
 template <int CD>
 __device__ __forceinline__ bool grad_pair(const GeoRec &q, const float (&col)[CD], float px,
-                                          float py0, float py1, int32_t idx, BwdPix<CD> &s0,
+                                          float2 npy, int32_t idx, BwdPix<CD> &s0,
                                           BwdPix<CD> &s1, float (&g)[7 + CD]) {
-    const float dx = q.x - px, dy0 = q.y - py0, dy1 = q.y - py1;
-    const float sg0 = (q.cxx * dx * dx + q.cyy * dy0 * dy0) + 2.f * q.cxy * dx * dy0;
-    const float sg1 = (q.cxx * dx * dx + q.cyy * dy1 * dy1) + 2.f * q.cxy * dx * dy1;
-    const bool v0 = s0.inside && idx <= s0.bin && !(sg0 < 0.f || sg0 >= 1.f);
-    const bool v1 = s1.inside && idx <= s1.bin && !(sg1 < 0.f || sg1 >= 1.f);
+    const float dx = q.x - px;
+    const float2 dy = __fadd2_rn(make_float2(q.y, q.y), npy);
+    const float A = q.cxx * dx * dx;
+    const float B = 2.f * q.cxy * dx;
+    float2 sg = __fmul2_rn(make_float2(q.cyy, q.cyy), dy);
+    sg = __ffma2_rn(sg, dy, make_float2(A, A));
+    sg = __ffma2_rn(make_float2(B, B), dy, sg);
+    const bool v0 = s0.inside && idx <= s0.bin && !(sg.x < 0.f || sg.x >= 1.f);
+    const bool v1 = s1.inside && idx <= s1.bin && !(sg.y < 0.f || sg.y >= 1.f);
     if (!__any_sync(0xffffffffu, v0 || v1)) return false;
+    float2 om = __ffma2_rn(sg, make_float2(-1.f, -1.f), make_float2(1.f, 1.f));
+    om.x = v0 ? om.x : 1.f;
+    om.y = v1 ? om.y : 1.f;
+    const float2 l = make_float2(__log2f(om.x), __log2f(om.y));
+    const float2 e = __fmul2_rn(l, make_float2(q.beta, q.beta));
+    const float2 vis = make_float2(exp2f(e.x), exp2f(e.y));
+    const float2 ov = __fmul2_rn(make_float2(q.opac, q.opac), vis);
+    const float2 alpha = make_float2(fminf(0.999f, ov.x), fminf(0.999f, ov.y));
+    const float2 oma = __ffma2_rn(alpha, make_float2(-1.f, -1.f), make_float2(1.f, 1.f));
+    const float2 ra = make_float2(1.0f / oma.x, 1.0f / oma.y);
+    const float2 Tn = __fmul2_rn(make_float2(s0.T, s1.T), ra);
+    float2 fac = __fmul2_rn(alpha, Tn);
+    fac.x = v0 ? fac.x : 0.f;
+    fac.y = v1 ? fac.y : 0.f;
+    float2 cv = __fmul2_rn(make_float2(col[0], col[0]), make_float2(s0.vrc[0], s1.vrc[0]));
 #pragma unroll
-    for (int u = 0; u < 7 + CD; ++u) g[u] = 0.f;
-    grad_px<CD>(q, col, dx, dy0, sg0, v0, s0, g);
-    grad_px<CD>(q, col, dx, dy1, sg1, v1, s1, g);
+    for (int k = 1; k < CD; ++k)
+        cv = __ffma2_rn(make_float2(col[k], col[k]), make_float2(s0.vrc[k], s1.vrc[k]), cv);
+#pragma unroll
+    for (int k = 0; k < CD; ++k) {
+        const float2 gc = __fmul2_rn(fac, make_float2(s0.vrc[k], s1.vrc[k]));
+        g[7 + k] = gc.x + gc.y;
+    }
+    const float2 kms = __fadd2_rn(make_float2(s0.K, s1.K), make_float2(-s0.S, -s1.S));
+    float2 va = __ffma2_rn(Tn, cv, __fmul2_rn(ra, kms));
+    va.x = (v0 && ov.x <= 0.999f) ? va.x : 0.f;
+    va.y = (v1 && ov.y <= 0.999f) ? va.y : 0.f;
+    const float2 u = __fmul2_rn(vis, va);
+    const float2 w = __fmul2_rn(u, make_float2(__fdividef(1.f, om.x), __fdividef(1.f, om.y)));
+    const float ws = w.x + w.y;
+    const float2 wdy = __fmul2_rn(w, dy);
+    const float2 wdy2 = __fmul2_rn(wdy, dy);
+    const float2 ul = __fmul2_rn(u, l);
+    g[0] = ws * dx;
+    g[1] = wdy.x + wdy.y;
+    g[2] = ws * (dx * dx);
+    g[3] = g[1] * dx;
+    g[4] = wdy2.x + wdy2.y;
+    g[5] = u.x + u.y;
+    g[6] = ul.x + ul.y;
+    const float2 S = __ffma2_rn(fac, cv, make_float2(s0.S, s1.S));
+    s0.S = S.x;
+    s1.S = S.y;
+    s0.T = v0 ? Tn.x : s0.T;
+    s1.T = v1 ? Tn.y : s1.T;
     return true;
 }
 
-// Factor turning the reduced sum g[u] of a record into its gradient value u of
-// [v_xy(2), v_conic(3), v_opacity, v_beta, v_colour(CD)].
+// Factor turning the reduced sum g[u] (u >= 2) of a record into its gradient
+// value u of [v_xy(2), v_conic(3), v_opacity, v_beta, v_colour(CD)]; v_xy is
+// -2 opacity beta (conic [w dx, w dy]) and is formed at the flush.
 __device__ __forceinline__ float record_scale(int u, float opac, float beta) {
     const float ob = opac * beta;
-    if (u < 2) return -2.f * ob;
     if (u == 3) return -2.f * ob;
     if (u < 5) return -ob;
     if (u == 6) return opac * 0.6931471805599453f;
@@ -609,6 +625,7 @@ __global__ void __launch_bounds__(512) raster_bwd_kernel(RasterArgs a) {
     re = max(rs, min(re, T_all));
 
     const float px = (float)j + 0.5f, py0 = (float)i0 + 0.5f, py1 = py0 + 1.f;
+    const float2 npy = make_float2(-py0, -py1);
     BwdPix<CD> s0, s1;
     bwd_pix_init<CD>(s0, a, pix0, in0, bg);
     bwd_pix_init<CD>(s1, a, pix1, in1, bg);
@@ -657,6 +674,11 @@ __global__ void __launch_bounds__(512) raster_bwd_kernel(RasterArgs a) {
         const float be0 = (tid < cnt) ? batch[tid].beta : 0.f;
         const float op1 = (tid + NT < cnt) ? batch[tid + NT].opac : 0.f;
         const float be1 = (tid + NT < cnt) ? batch[tid + NT].beta : 0.f;
+        const float3 cn0 = (tid < cnt) ? make_float3(batch[tid].cxx, batch[tid].cxy, batch[tid].cyy)
+                                       : make_float3(0.f, 0.f, 0.f);
+        const float3 cn1 = (tid + NT < cnt) ? make_float3(batch[tid + NT].cxx, batch[tid + NT].cxy,
+                                                          batch[tid + NT].cyy)
+                                            : make_float3(0.f, 0.f, 0.f);
         build_masks(batch, cnt, lo, NT, nw, wpr, tx * a.TS, ty * a.TS, tid, lane, wmask, wbin);
         if (!PACK) {
 #pragma unroll
@@ -684,7 +706,7 @@ __global__ void __launch_bounds__(512) raster_bwd_kernel(RasterArgs a) {
                 float col[CD];
                 load_color<CD, PACK>(scol4, scol, buf * BR + t, col);
                 float g[NV];
-                if (!grad_pair<CD>(q, col, px, py0, py1, idx, s0, s1, g)) continue;
+                if (!grad_pair<CD>(q, col, px, npy, idx, s0, s1, g)) continue;
                 ReduceChunks<0, NV>::run(g, lane, gacc + t * NV);
                 if (lane == 0) touched[t] = 1;
             }
@@ -696,10 +718,14 @@ __global__ void __launch_bounds__(512) raster_bwd_kernel(RasterArgs a) {
             if (sl < cnt && touched[sl]) {
                 const int64_t gg = half ? gid1 : gid0;
                 const float op = half ? op1 : op0, be = half ? be1 : be0;
+                const float3 cn = half ? cn1 : cn0;
                 float *ga = gacc + sl * NV;
+                const float f2 = -2.f * op * be;
+                const float m0 = f2 * (cn.x * ga[0] + cn.y * ga[1]);
+                const float m1 = f2 * (cn.y * ga[0] + cn.z * ga[1]);
 #pragma unroll
                 for (int u = 0; u < NV; ++u) {
-                    const float val = ga[u] * record_scale(u, op, be);
+                    const float val = u == 0 ? m0 : u == 1 ? m1 : ga[u] * record_scale(u, op, be);
                     if (val != 0.f) {
                         float *dst;
                         if (u < 2) dst = a.v_m2 + 2 * gg + u;
