@@ -133,6 +133,20 @@ class ClockSampler:
                 "samples": len(used), "window": "timed region" if used is inside else "run"}
 
 
+def replica_throughput(ms, world, device):
+    """Whole-job step time and throughput of `world` independent replicas
+    (the path does not shard: every rank runs the same per-rank workload):
+    the job's step takes as long as its slowest rank."""
+    ms_max = ms
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+        dist.barrier()
+    return ms_max, world * 1000.0 / ms_max
+
+
 def l2_flush_buffer(dev):
     return torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
@@ -618,14 +632,7 @@ def main():
     # library kernels, once per replay (the host-side counter sees the capture)
     launches = gs.launches_per_replay * args.steps
     torch.cuda.synchronize()
-    ms_max = ms
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
-        dist.barrier()
-    value = world * 1000.0 / ms_max
+    ms_max, value = replica_throughput(ms, world, dev)
     kernel_ms = {k: t / args.steps for k, (n, t) in kernels.items()}
 
     # end to end through the public API: parameters and target copied from
@@ -647,7 +654,7 @@ def main():
         e2e_step()
     e2e_ms = time_steps(e2e_step, args.steps, dev, flush)
     gs.check()
-    e2e_val = world * 1000.0 / e2e_ms
+    _, e2e_val = replica_throughput(e2e_ms, world, dev)
     clocks.stop()
     # the same step without the graph (one launch per kernel from the host)
     fz.prime()

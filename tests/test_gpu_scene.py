@@ -150,3 +150,26 @@ def test_graphed_step_matches_eager_and_follows_parameter_updates():
         with torch.no_grad():  # an in-place parameter update, as an optimizer makes
             for v in leaves.values():
                 v.add_(0.01 * torch.randn_like(v))
+
+
+def test_kernel_timer_eager_and_graph_replays():
+    from ubs import _lib as L
+    from ubs.render import GraphedStep
+    p = make_params(3000, 6, seed=41)
+    cam = S.orbit_view(4, 3.0, 160, 120, 140.0, 140.0, device=DEV)
+    views = Views([cam], device=DEV)
+    leaves = {k: v.clone().requires_grad_(True) for k, v in p.items()}
+    L.profile_start(256)
+    colors, alphas = Renderer(dim=6).render(leaves, views)
+    (colors.sum() + alphas.sum()).backward()
+    k = L.profile_stop()
+    for name in ("scene_prim_fwd", "scene_emit", "bucket_sort_warp", "scene_gather", "raster_fwd",
+                 "raster_bwd", "scene_prim_bwd"):
+        assert name in k and k[name][0] >= 1 and k[name][1] > 0, (name, k.get(name))
+    gs = GraphedStep(Renderer(dim=6), leaves, views, None,
+                     lambda c, a: c.square().mean(), before_capture=lambda: L.profile_start(256))
+    for _ in range(3):
+        gs.replay()
+        L.profile_sample()
+    k = L.profile_stop()
+    assert k["raster_bwd"][0] == 3 and k["raster_fwd"][0] == 3 and k["raster_bwd"][1] > 0
