@@ -166,7 +166,9 @@ def test_kernel_timer_eager_and_graph_replays():
     for name in ("scene_prim_fwd", "scene_emit", "bucket_sort_warp", "scene_gather", "raster_fwd",
                  "raster_bwd", "scene_prim_bwd"):
         assert name in k and k[name][0] >= 1 and k[name][1] > 0, (name, k.get(name))
-    gs = GraphedStep(Renderer(dim=6), leaves, views, None,
+    # fresh leaves: these went through an eager backward on the default stream
+    leaves_g = {k: v.detach().clone().requires_grad_(True) for k, v in p.items()}
+    gs = GraphedStep(Renderer(dim=6), leaves_g, views, None,
                      lambda c, a: c.square().mean(), before_capture=lambda: L.profile_start(256))
     for _ in range(3):
         gs.replay()

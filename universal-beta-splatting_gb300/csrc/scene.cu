@@ -67,6 +67,7 @@ struct SceneArgs {
     float tile_size, eps2d, near_p, far_p, radius_clip;
     // outputs / workspace
     Rec *recs;
+    float4 *cols_n; // colour row per primitive (written by the view-0 entries)
     int32_t *radius;
     float *depth;
     int32_t *bucket_counts;
@@ -215,6 +216,8 @@ template <int D> __global__ void scene_prim_fwd_kernel(SceneArgs a) {
     float4 *dst = reinterpret_cast<float4 *>(a.recs + idx);
     dst[0] = make_float4(r.x, r.y, r.opac, r.beta);
     dst[1] = make_float4(r.cxx, r.cxy, r.cyy, __int_as_float(r.gid));
+    if (v == 0) // one colour row per primitive for the sorted-record gather
+        a.cols_n[n] = make_float4(a.rgb[n * 3], a.rgb[n * 3 + 1], a.rgb[n * 3 + 2], 0.f);
     a.radius[idx] = p.radius;
     a.depth[idx] = p.radius > 0 ? p.depth : 0.f;
     if (p.radius <= 0) return;
@@ -315,7 +318,7 @@ struct KeyWriter {
 __global__ void __launch_bounds__(256) scene_gather_kernel(const uint64_t *__restrict__ keys,
                                                            const int64_t *T_dev, int64_t cap,
                                                            const Rec *__restrict__ recs_in,
-                                                           const float *__restrict__ rgb,
+                                                           const float4 *__restrict__ cols_n,
                                                            int64_t N, Rec *__restrict__ recs_out,
                                                            float4 *__restrict__ cols_out) {
     const int64_t T = imin64(*T_dev, cap);
@@ -324,8 +327,7 @@ __global__ void __launch_bounds__(256) scene_gather_kernel(const uint64_t *__res
         const int64_t gid = (int64_t)(keys[i] & 0xffffffffu);
         const float4 *src = reinterpret_cast<const float4 *>(recs_in + gid);
         const float4 a = src[0], b = src[1];
-        const int64_t n = gid % N;
-        const float4 c = make_float4(rgb[n * 3], rgb[n * 3 + 1], rgb[n * 3 + 2], 0.f);
+        const float4 c = cols_n[gid % N];
         float4 *dst = reinterpret_cast<float4 *>(recs_out + i);
         dst[0] = a;
         dst[1] = b;
@@ -466,6 +468,7 @@ struct SceneWs {
     uint64_t *keys, *scratch;
     Rec *sorted;
     float4 *cols;
+    float4 *cols_n;
     float *grads; // v_m2 (2), v_cn (3), v_col (3), v_op, v_be per (view, primitive)
     size_t bytes;
 };
@@ -494,6 +497,7 @@ SceneWs scene_ws(void *base, int32_t C, int64_t N, int32_t nb, int64_t cap) {
     w.scratch = reinterpret_cast<uint64_t *>(take(cap * 8));
     w.sorted = reinterpret_cast<Rec *>(take(cap * sizeof(Rec)));
     w.cols = reinterpret_cast<float4 *>(take(cap * 16));
+    w.cols_n = reinterpret_cast<float4 *>(take((size_t)N * 16));
     w.grads = reinterpret_cast<float *>(take(CN * 10 * 4));
     w.bytes = o;
     return w;
@@ -584,6 +588,7 @@ int ubs_scene_forward(int32_t dim, int64_t N, const float *xyz, const float *mea
         cudaMemsetAsync(w.bucket_counts, 0, (size_t)n_buckets * 4, st) != cudaSuccess)
         return check_launch("scene_forward memset");
     a.recs = w.recs;
+    a.cols_n = w.cols_n;
     a.radius = w.radius;
     a.depth = w.depth;
     a.bucket_counts = w.bucket_counts;
@@ -620,7 +625,8 @@ int ubs_scene_forward(int32_t dim, int64_t N, const float *xyz, const float *mea
                                                (int64_t)1 << 20);
         UBS_TIMED("scene_gather", st,
                   scene_gather_kernel<<<grid, 256, 0, st>>>(w.keys, &w.hdr->total, capacity,
-                                                            w.recs, rgb, N, w.sorted, w.cols));
+                                                            w.recs, w.cols_n, N, w.sorted,
+                                                            w.cols));
         note_launch();
         if (int e = check_launch("scene_gather")) return e;
     }

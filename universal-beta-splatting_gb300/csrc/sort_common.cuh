@@ -214,40 +214,50 @@ static __global__ void __launch_bounds__(1024) bucket_order_kernel(const int32_t
 
 // Bitonic sort of the 32 * E keys of a warp held E per lane in registers,
 // blocked (element i = lane * E + e): exchange distances below E stay inside
-// a lane, larger ones are lane-xor shuffles.  Fully unrolled, so the key
-// arrays stay in registers.
+// a lane, larger ones are lane-xor shuffles.  Only the loop over a lane's E
+// elements is unrolled (so the key arrays stay in registers); the stage loops
+// run at run time, with one unrolled body per in-lane distance, which keeps
+// the code small enough for the instruction cache.
+template <int E, int J>
+__device__ __forceinline__ void bitonic_in_lane(uint64_t (&v)[E], int lane, int k) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int p = e ^ J;
+        if (p > e) {
+            const bool up = (((lane * E + e) & k) == 0);
+            const uint64_t a = v[e], b = v[p];
+            const bool sw = (a > b) == up;
+            v[e] = sw ? b : a;
+            v[p] = sw ? a : b;
+        }
+    }
+}
+
 template <int E>
 __device__ __forceinline__ void warp_bitonic(uint64_t (&v)[E], int lane) {
     constexpr int N = 32 * E;
-#pragma unroll
+#pragma unroll 1
     for (int k = 2; k <= N; k <<= 1) {
+#pragma unroll 1
+        for (int j = k >> 1; j >= E; j >>= 1) { // across lanes
+            const int lj = j / E;
+            const bool lower = (lane & lj) == 0;
 #pragma unroll
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            if (j < E) {
-#pragma unroll
-                for (int e = 0; e < E; ++e) {
-                    const int p = e ^ j;
-                    if (p > e) {
-                        const bool up = (((lane * E + e) & k) == 0);
-                        const uint64_t a = v[e], b = v[p];
-                        const bool sw = (a > b) == up;
-                        v[e] = sw ? b : a;
-                        v[p] = sw ? a : b;
-                    }
-                }
-            } else {
-                const int lj = j / E;
-                const bool lower = (lane & lj) == 0;
-#pragma unroll
-                for (int e = 0; e < E; ++e) {
-                    const uint64_t o = __shfl_xor_sync(0xffffffffu, v[e], lj);
-                    const bool up = (((lane * E + e) & k) == 0);
-                    const bool keep_min = lower == up;
-                    const bool o_less = o < v[e];
-                    v[e] = (keep_min == o_less) ? o : v[e];
-                }
+            for (int e = 0; e < E; ++e) {
+                const uint64_t o = __shfl_xor_sync(0xffffffffu, v[e], lj);
+                const bool up = (((lane * E + e) & k) == 0);
+                const bool keep_min = lower == up;
+                const bool o_less = o < v[e];
+                v[e] = (keep_min == o_less) ? o : v[e];
             }
         }
+        // inside a lane: distances min(k / 2, E / 2) .. 1
+        const int jmax = (k >> 1) < E ? (k >> 1) : (E >> 1);
+        if (E >= 32 && jmax >= 16) bitonic_in_lane<E, (E >= 32 ? 16 : 1)>(v, lane, k);
+        if (E >= 16 && jmax >= 8) bitonic_in_lane<E, (E >= 16 ? 8 : 1)>(v, lane, k);
+        if (E >= 8 && jmax >= 4) bitonic_in_lane<E, (E >= 8 ? 4 : 1)>(v, lane, k);
+        if (E >= 4 && jmax >= 2) bitonic_in_lane<E, (E >= 4 ? 2 : 1)>(v, lane, k);
+        if (E >= 2 && jmax >= 1) bitonic_in_lane<E, 1>(v, lane, k);
     }
 }
 

@@ -276,7 +276,10 @@ class GraphedStep:
     `loss` holds its value.  The intersection capacity is fixed when the step
     is captured (the first frame's count times `headroom`); `check()` reads the
     last replay's count back and raises if the frame overflowed, in which case
-    the step must be captured again."""
+    the step must be captured again.  Capture on parameter tensors that have
+    not been through an eager backward on the default stream (or on fresh
+    copies of them): PyTorch's gradient accumulation for such leaves would
+    make the capture wait on that stream, which capture does not allow."""
 
     def __init__(self, renderer: Renderer, params: Dict[str, torch.Tensor], views: Views,
                  backgrounds: Optional[torch.Tensor], loss_fn, headroom: float = 1.5,
