@@ -175,3 +175,26 @@ def test_kernel_timer_eager_and_graph_replays():
         L.profile_sample()
     k = L.profile_stop()
     assert k["raster_bwd"][0] == 3 and k["raster_fwd"][0] == 3 and k["raster_bwd"][1] > 0
+
+
+@pytest.mark.parametrize("ts", [8, 24, 32])
+def test_fused_tile_sizes_match_dropin(ts):
+    from gsplat.cuda import _wrapper as Wr
+    p = make_params(4000, 6, seed=50 + ts)
+    cam = S.orbit_view(6, 3.0, 250, 170, 220.0, 220.0, device=DEV)
+    bg = torch.tensor([0.3, 0.2, 0.1], device=DEV)
+    ri, rj = S.rest_indices(6, DEV)
+    leaves_d = {k: v.detach().clone().requires_grad_(True) for k, v in p.items()}
+    img_d, _, _ = S.render_view(leaves_d, cam, bg, ri, rj, tile_size=ts)
+    img_d = img_d.permute(1, 2, 0)
+    r = Renderer(dim=6, tile_size=ts)
+    views = Views([cam], tile_size=ts, device=DEV)
+    leaves_f = {k: v.detach().clone().requires_grad_(True) for k, v in p.items()}
+    colors, _ = r.render(leaves_f, views, bg)
+    img_f = views.split(colors)[0]
+    assert float((img_f - img_d).detach().abs().max()) < 1e-5
+    w = torch.randn(170, 250, 3, generator=torch.Generator().manual_seed(1)).to(DEV)
+    (img_d * w).sum().backward()
+    (img_f * w).sum().backward()
+    for k in leaves_d:
+        assert rel_l2(leaves_f[k].grad, leaves_d[k].grad) < 1e-4, k
