@@ -670,7 +670,10 @@ def main():
     d_step = lambda: gpu_step(p, cam, ri, rj, bg, target)  # noqa: E731
     for _ in range(3):
         d_step()
+    L.profile_start(64 * (K2 + 1))
     d_ms = time_steps(d_step, K2, dev, flush)
+    d_kernels = {k: round(t / K2, 4) for k, (n, t) in
+                 sorted(L.profile_stop().items(), key=lambda x: -x[1][1])}
 
     def d_fwd():
         from ubs import scene as S
@@ -781,7 +784,7 @@ def main():
             "eager": {"value": 1000.0 / eager_ms, "unit": "it/s", "ms_per_step": eager_ms,
                       "what": "the same fused step launched kernel by kernel (no graph)"},
             "dropin": {"value": 1000.0 / d_ms, "unit": "it/s", "ms_per_step": d_ms,
-                       "render_fps": 1000.0 / d_fwd_ms,
+                       "render_fps": 1000.0 / d_fwd_ms, "kernels_ms_per_step": d_kernels,
                        "what": "the same step through the drop-in gsplat operators"},
             "clocks": clocks.summary(clocks.marks.get("t0", 0), clocks.marks.get("t1", 0)),
             "kernels_ms_per_step": {k: round(v, 4) for k, v in

@@ -143,20 +143,22 @@ __global__ void isect_emit_bucket_kernel(int64_t CN, int64_t N, const float2 *__
                                          uint64_t *__restrict__ keys, int64_t cap,
                                          uint32_t *status) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= CN) return;
-    const int32_t rad = radii[idx];
-    if (rad <= 0) return;
-    const float2 m = means2d[idx];
-    const Box b = tile_box(m.x, m.y, rad, ts, tw, th);
-    const uint64_t key = ((uint64_t)(uint32_t)__float_as_int(depths[idx]) << 32) | (uint64_t)idx;
-    const int64_t cam = idx / N;
-    int32_t *cur = cursor + cam * (int64_t)tw * th;
-    for (uint32_t y = b.y0; y < b.y1; ++y)
-        for (uint32_t x = b.x0; x < b.x1; ++x) {
-            const int32_t pos = atomicAdd(&cur[y * tw + x], 1);
-            if (pos >= 0 && pos < cap) keys[pos] = key;
-            else atomicOr(status, DEV_ERR_OVERFLOW);
+    const int lane = threadIdx.x & 31;
+    uint32_t n = 0, bw = 1;
+    int32_t *cur = cursor;
+    uint64_t key = 0;
+    if (idx < CN && radii[idx] > 0) {
+        const float2 m = means2d[idx];
+        const Box b = tile_box(m.x, m.y, radii[idx], ts, tw, th);
+        if (b.x1 > b.x0 && b.y1 > b.y0) {
+            bw = b.x1 - b.x0;
+            n = bw * (b.y1 - b.y0);
+            const int64_t cam = idx / N;
+            cur = cursor + cam * (int64_t)tw * th + (int64_t)b.y0 * tw + b.x0;
+            key = ((uint64_t)(uint32_t)__float_as_int(depths[idx]) << 32) | (uint64_t)idx;
         }
+    }
+    warp_emit_rects(n, bw, tw, cur, key, lane, keys, cap, status);
 }
 
 // reference generation order: primitive by primitive, tiles row-major

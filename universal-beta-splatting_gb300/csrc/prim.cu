@@ -26,9 +26,30 @@ __global__ void rotmat_bwd_kernel(int64_t n, const float *__restrict__ g, float 
     vl[i * 3 + 2] = r[5] - r[7];
 }
 
+// ------------------------------------------------- coalesced output rows
+// The per-primitive outputs are [n, w] rows, one per thread; stored directly,
+// every warp store would touch 32 different sectors.  Kernels with rows of
+// up to 49 floats stage a block's rows in shared memory (rows padded to an odd
+// stride, so a thread's own writes are free of bank conflicts) and copy them
+// out with consecutive threads on consecutive floats.
+constexpr int ROW_BLOCK = 128;
+template <int W> struct RowBuf {
+    static constexpr int S = W | 1;
+    float v[ROW_BLOCK * S];
+    __device__ __forceinline__ float &at(int t, int k) { return v[t * S + k]; }
+    // after a barrier: rows [0, cnt) to dst rows [i0, i0 + cnt)
+    __device__ __forceinline__ void flush(float *__restrict__ dst, int64_t i0, int cnt) const {
+        float *d = dst + i0 * W;
+        for (int e = threadIdx.x; e < cnt * W; e += blockDim.x) {
+            const int t = e / W;
+            d[e] = v[t * S + (e - t * W)];
+        }
+    }
+};
+
 // ------------------------------------------------------------------ a3
 template <int D>
-__global__ void covar_fwd_kernel(int64_t n, const float *__restrict__ rot,
+__global__ void __launch_bounds__(ROW_BLOCK) covar_fwd_kernel(int64_t n, const float *__restrict__ rot,
                                  const float *__restrict__ scale, const float *__restrict__ ltri,
                                  const int32_t *__restrict__ ri_g, const int32_t *__restrict__ rj_g,
                                  int m_rest, int spatial, float *__restrict__ covar) {
@@ -37,50 +58,64 @@ __global__ void covar_fwd_kernel(int64_t n, const float *__restrict__ rot,
         ri[m] = ri_g[m];
         rj[m] = rj_g[m];
     }
+    constexpr bool STAGE = D <= 7;
+    __shared__ RowBuf<STAGE ? D * D : 1> full;
+    __shared__ RowBuf<STAGE ? 9 : 1> block3;
     __syncthreads();
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    constexpr int full_m = D * (D - 1) / 2;
-    float L[D * D];
-    build_L<D>(rot + i * 9, scale + i * D, ltri + i * full_m + 3, ri, rj, m_rest, L);
-    if (spatial || D == 3) {
-        float *o = covar + i * 9;
+    const int t = threadIdx.x;
+    const int64_t i0 = (int64_t)blockIdx.x * blockDim.x, i = i0 + t;
+    const int cnt = (int)(n - i0 < (int64_t)blockDim.x ? n - i0 : (int64_t)blockDim.x);
+    const bool sp = spatial || D == 3;
+    if (i < n) {
+        constexpr int full_m = D * (D - 1) / 2;
+        float L[D * D];
+        build_L<D>(rot + i * 9, scale + i * D, ltri + i * full_m + 3, ri, rj, m_rest, L);
+        if (sp) {
 #pragma unroll
-        for (int r = 0; r < 3; ++r)
+            for (int r = 0; r < 3; ++r)
 #pragma unroll
-            for (int c = 0; c < 3; ++c)
-                o[r * 3 + c] = L[r * D] * L[c * D] + L[r * D + 1] * L[c * D + 1] +
-                               L[r * D + 2] * L[c * D + 2];
-        return;
-    }
-    float *o = covar + i * D * D;
+                for (int c = 0; c < 3; ++c) {
+                    const float v = L[r * D] * L[c * D] + L[r * D + 1] * L[c * D + 1] +
+                                    L[r * D + 2] * L[c * D + 2];
+                    if (STAGE) block3.at(t, r * 3 + c) = v;
+                    else covar[i * 9 + r * 3 + c] = v;
+                }
+        } else {
 #pragma unroll
-    for (int r = 0; r < D; ++r)
+            for (int r = 0; r < D; ++r)
 #pragma unroll
-        for (int c = 0; c <= r; ++c) {
-            float acc = 0.f;
+                for (int c = 0; c <= r; ++c) {
+                    float acc = 0.f;
 #pragma unroll
-            for (int k = 0; k < D; ++k) acc += L[r * D + k] * L[c * D + k];
-            o[r * D + c] = acc;
-            o[c * D + r] = acc;
+                    for (int k = 0; k < D; ++k) acc += L[r * D + k] * L[c * D + k];
+                    if (STAGE) {
+                        full.at(t, r * D + c) = acc;
+                        full.at(t, c * D + r) = acc;
+                    } else {
+                        covar[i * D * D + r * D + c] = acc;
+                        covar[i * D * D + c * D + r] = acc;
+                    }
+                }
         }
+    }
+    if (!STAGE) return;
+    __syncthreads();
+    if (sp) block3.flush(covar, i0, cnt);
+    else full.flush(covar, i0, cnt);
 }
 
+// One primitive of covar_bwd_kernel: rows go to the shared row buffers when
+// given (strides 9|1, D|1, full_m|1), else straight to global memory.
 template <int D>
-__global__ void covar_bwd_kernel(int64_t n, const float *__restrict__ rot,
-                                 const float *__restrict__ scale, const float *__restrict__ ltri,
-                                 const int32_t *__restrict__ ri_g, const int32_t *__restrict__ rj_g,
-                                 int m_rest, int spatial, const float *__restrict__ v_covar,
-                                 float *__restrict__ v_rot, float *__restrict__ v_scale,
-                                 float *__restrict__ v_ltri) {
-    __shared__ int32_t ri[64], rj[64];
-    for (int m = threadIdx.x; m < m_rest && m < 64; m += blockDim.x) {
-        ri[m] = ri_g[m];
-        rj[m] = rj_g[m];
-    }
-    __syncthreads();
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__device__ __forceinline__ void covar_bwd_row(int64_t i, int t, const float *__restrict__ rot,
+                                              const float *__restrict__ scale,
+                                              const float *__restrict__ ltri, const int32_t *ri,
+                                              const int32_t *rj, int m_rest, int spatial,
+                                              const float *__restrict__ v_covar,
+                                              float *__restrict__ v_rot,
+                                              float *__restrict__ v_scale,
+                                              float *__restrict__ v_ltri, float *stR, float *stS,
+                                              float *stL) {
     constexpr int full_m = D * (D - 1) / 2;
     const int dim = (spatial || D == 3) ? 3 : D;
     const float *R = rot + i * 9;
@@ -88,9 +123,9 @@ __global__ void covar_bwd_kernel(int64_t n, const float *__restrict__ rot,
     float L[D * D];
     build_L<D>(R, s, ltri + i * full_m + 3, ri, rj, m_rest, L);
     const float *G = v_covar + i * dim * dim;
-    float *gR = v_rot + i * 9;
-    float *gs = v_scale + i * D;
-    float *gl = v_ltri + i * full_m;
+    float *gR = stR ? stR + t * (9 | 1) : v_rot + i * 9;
+    float *gs = stS ? stS + t * (D | 1) : v_scale + i * D;
+    float *gl = stL ? stL + t * (full_m | 1) : v_ltri + i * full_m;
     // dL = (G + G^T) L over the output rows
     float dL[D * D];
 #pragma unroll
@@ -127,6 +162,38 @@ __global__ void covar_bwd_kernel(int64_t n, const float *__restrict__ rot,
     }
 }
 
+template <int D>
+__global__ void __launch_bounds__(ROW_BLOCK) covar_bwd_kernel(int64_t n, const float *__restrict__ rot,
+                                 const float *__restrict__ scale, const float *__restrict__ ltri,
+                                 const int32_t *__restrict__ ri_g, const int32_t *__restrict__ rj_g,
+                                 int m_rest, int spatial, const float *__restrict__ v_covar,
+                                 float *__restrict__ v_rot, float *__restrict__ v_scale,
+                                 float *__restrict__ v_ltri) {
+    __shared__ int32_t ri[64], rj[64];
+    for (int m = threadIdx.x; m < m_rest && m < 64; m += blockDim.x) {
+        ri[m] = ri_g[m];
+        rj[m] = rj_g[m];
+    }
+    constexpr int full_m = D * (D - 1) / 2;
+    constexpr bool STAGE = D <= 7;
+    __shared__ RowBuf<STAGE ? 9 : 1> sR;
+    __shared__ RowBuf<STAGE ? D : 1> sS;
+    __shared__ RowBuf<STAGE ? full_m : 1> sL;
+    __syncthreads();
+    const int t = threadIdx.x;
+    const int64_t i0 = (int64_t)blockIdx.x * blockDim.x, i = i0 + t;
+    const int cnt = (int)(n - i0 < (int64_t)blockDim.x ? n - i0 : (int64_t)blockDim.x);
+    if (i < n)
+        covar_bwd_row<D>(i, t, rot, scale, ltri, ri, rj, m_rest, spatial, v_covar, v_rot, v_scale,
+                         v_ltri, STAGE ? sR.v : nullptr, STAGE ? sS.v : nullptr,
+                         STAGE ? sL.v : nullptr);
+    if (!STAGE) return;
+    __syncthreads();
+    sR.flush(v_rot, i0, cnt);
+    sS.flush(v_scale, i0, cnt);
+    sL.flush(v_ltri, i0, cnt);
+}
+
 // ------------------------------------------------------------------ a4
 template <int K>
 __global__ void cond_fwd_kernel(int64_t n, const float *__restrict__ means,
@@ -150,17 +217,21 @@ __global__ void cond_fwd_kernel(int64_t n, const float *__restrict__ means,
     cond_forward<K>(m, V, opac[i], b, q, om + i * 3, oV + i * 9, oo + i);
 }
 
+// One primitive of cond_bwd_kernel: the [D, D] and [D] gradient rows go to the
+// shared row buffers when given (strides (D*D)|1 and D|1), else to global memory.
 template <int K>
-__global__ void cond_bwd_kernel(int64_t n, const float *__restrict__ means,
-                                const float *__restrict__ covars, const float *__restrict__ opac,
-                                const float *__restrict__ betas, const float *__restrict__ query,
-                                const float *__restrict__ vm, const float *__restrict__ vV,
-                                const float *__restrict__ vo, float *__restrict__ gm,
-                                float *__restrict__ gV, float *__restrict__ go,
-                                float *__restrict__ gb, int exact) {
+__device__ __forceinline__ void cond_bwd_row(int64_t i, int t, const float *__restrict__ means,
+                                             const float *__restrict__ covars,
+                                             const float *__restrict__ opac,
+                                             const float *__restrict__ betas,
+                                             const float *__restrict__ query,
+                                             const float *__restrict__ vm,
+                                             const float *__restrict__ vV,
+                                             const float *__restrict__ vo,
+                                             float *__restrict__ gm, float *__restrict__ gV,
+                                             float *__restrict__ go, float *__restrict__ gb,
+                                             int exact, float *stV, float *stM) {
     constexpr int D = K + 3;
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
     float m[D], V[D * D], b[K], q[K], gM[3], gVc[9];
 #pragma unroll
     for (int k = 0; k < D; ++k) m[k] = means[i * D + k];
@@ -177,13 +248,38 @@ __global__ void cond_bwd_kernel(int64_t n, const float *__restrict__ means,
     for (int k = 0; k < 9; ++k) gVc[k] = vV[i * 9 + k];
     float lm[D], lV[D * D], lb[K], lo;
     cond_backward<K>(m, V, opac[i], b, q, gM, gVc, vo[i], exact != 0, lm, lV, &lo, lb);
+    float *dm = stM ? stM + t * (D | 1) : gm + i * D;
+    float *dV = stV ? stV + t * ((D * D) | 1) : gV + i * D * D;
 #pragma unroll
-    for (int k = 0; k < D; ++k) gm[i * D + k] = lm[k];
+    for (int k = 0; k < D; ++k) dm[k] = lm[k];
 #pragma unroll
-    for (int k = 0; k < D * D; ++k) gV[i * D * D + k] = lV[k];
+    for (int k = 0; k < D * D; ++k) dV[k] = lV[k];
     go[i] = lo;
 #pragma unroll
     for (int k = 0; k < K; ++k) gb[i * K + k] = lb[k];
+}
+
+
+template <int K>
+__global__ void __launch_bounds__(ROW_BLOCK) cond_bwd_kernel(
+    int64_t n, const float *__restrict__ means, const float *__restrict__ covars,
+    const float *__restrict__ opac, const float *__restrict__ betas,
+    const float *__restrict__ query, const float *__restrict__ vm, const float *__restrict__ vV,
+    const float *__restrict__ vo, float *__restrict__ gm, float *__restrict__ gV,
+    float *__restrict__ go, float *__restrict__ gb, int exact) {
+    constexpr int D = K + 3;
+    constexpr bool STAGE = D <= 7;
+    __shared__ RowBuf<STAGE ? D * D : 1> sV;
+    __shared__ RowBuf<STAGE ? D : 1> sM;
+    const int t = threadIdx.x;
+    const int64_t i0 = (int64_t)blockIdx.x * blockDim.x, i = i0 + t;
+    const int cnt = (int)(n - i0 < (int64_t)blockDim.x ? n - i0 : (int64_t)blockDim.x);
+    if (i < n) cond_bwd_row<K>(i, t, means, covars, opac, betas, query, vm, vV, vo, gm, gV, go, gb,
+                               exact, STAGE ? sV.v : nullptr, STAGE ? sM.v : nullptr);
+    if (!STAGE) return;
+    __syncthreads();
+    sV.flush(gV, i0, cnt);
+    sM.flush(gm, i0, cnt);
 }
 
 // ------------------------------------------------------------------ a6

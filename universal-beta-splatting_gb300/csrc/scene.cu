@@ -269,39 +269,9 @@ __global__ void scene_emit_kernel(int64_t CN, int64_t N, const Rec *__restrict__
             pitch = TW;
         }
     }
-    // inclusive scan of the pair counts over the warp
-    uint32_t incl = n;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-    }
-    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    for (uint32_t base = 0; base < total; base += 32) {
-        const uint32_t j = base + lane;
-        // owner: first lane whose inclusive count exceeds j
-        int owner = 0;
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1) {
-            const uint32_t c = __shfl_sync(0xffffffffu, incl, owner + step - 1);
-            if (c <= j) owner += step;
-        }
-        const uint32_t o_incl = __shfl_sync(0xffffffffu, incl, owner);
-        const uint32_t o_n = __shfl_sync(0xffffffffu, n, owner);
-        const uint32_t o_bw = __shfl_sync(0xffffffffu, bw, owner);
-        const uint32_t o_pitch = __shfl_sync(0xffffffffu, pitch, owner);
-        const uint64_t o_key = __shfl_sync(0xffffffffu, key, owner);
-        int32_t *o_cur = reinterpret_cast<int32_t *>(
-            __shfl_sync(0xffffffffu, reinterpret_cast<uintptr_t>(cur), owner));
-        if (j < total) {
-            const uint32_t local = j - (o_incl - o_n);
-            const uint32_t ry = local / o_bw, rx = local - ry * o_bw;
-            const int32_t pos = atomicAdd(o_cur + (int64_t)ry * o_pitch + rx, 1);
-            if (pos >= 0 && pos < cap) keys[pos] = o_key;
-            else atomicOr(status, DEV_ERR_OVERFLOW);
-        }
-    }
+    warp_emit_rects(n, bw, pitch, cur, key, lane, keys, cap, status);
 }
+
 
 // Sorted-entry writer of the fused path: the sort leaves each sorted key in
 // place; scene_gather_kernel then writes the blend's packed records.

@@ -163,6 +163,50 @@ __device__ __forceinline__ void bucket_range(const int32_t *offsets, int64_t bkt
     if (hi < lo) hi = lo;
 }
 
+// Warp-flattened emission of sort keys: every lane holds the tile rectangle
+// of one (view, primitive) entry -- n tiles, bw columns, row pitch `pitch`,
+// cursor of its first tile `cur` -- and the warp walks the concatenation of
+// the 32 rectangles 32 (entry, tile) pairs per round, so its rounds follow the
+// warp's total tile count rather than its largest entry and the cursor
+// atomics of a round are independent.  Each pair takes the next slot of its
+// tile's cursor and stores the entry's key there (slots past `cap` set the
+// overflow bit instead).
+__device__ __forceinline__ void warp_emit_rects(uint32_t n, uint32_t bw, uint32_t pitch,
+                                                int32_t *cur, uint64_t key, int lane,
+                                                uint64_t *__restrict__ keys, int64_t cap,
+                                                uint32_t *status) {
+    uint32_t incl = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t j = base + lane;
+        int owner = 0; // first lane whose inclusive count exceeds j
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+            const uint32_t c = __shfl_sync(0xffffffffu, incl, owner + step - 1);
+            if (c <= j) owner += step;
+        }
+        const uint32_t o_incl = __shfl_sync(0xffffffffu, incl, owner);
+        const uint32_t o_n = __shfl_sync(0xffffffffu, n, owner);
+        const uint32_t o_bw = __shfl_sync(0xffffffffu, bw, owner);
+        const uint32_t o_pitch = __shfl_sync(0xffffffffu, pitch, owner);
+        const uint64_t o_key = __shfl_sync(0xffffffffu, key, owner);
+        int32_t *o_cur = reinterpret_cast<int32_t *>(
+            __shfl_sync(0xffffffffu, reinterpret_cast<uintptr_t>(cur), owner));
+        if (j < total) {
+            const uint32_t local = j - (o_incl - o_n);
+            const uint32_t ry = local / o_bw, rx = local - ry * o_bw;
+            const int32_t pos = atomicAdd(o_cur + (int64_t)ry * o_pitch + rx, 1);
+            if (pos >= 0 && pos < cap) keys[pos] = o_key;
+            else atomicOr(status, DEV_ERR_OVERFLOW);
+        }
+    }
+}
+
 // Heaviest-first order of the buckets for the blend (longest-processing-time
 // scheduling): one CTA counting-sorts the buckets by record count into
 // ORDER_BINS bins of 4 records (descending; counts >= 4 * ORDER_BINS share the
