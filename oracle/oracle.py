@@ -216,8 +216,10 @@ def isect_offset_encode(isect_ids, n_cameras, tile_width, tile_height):
 
 def rasterize_to_pixels(means2d, conics, colors, opacities, betas, width, height, tile_size,
                         isect_offsets, flatten_ids, backgrounds=None, masks=None,
-                        dtype=np.float32, row_step=1):
-    """row_step > 1 blends only every row_step-th tile row (a timing sample)."""
+                        dtype=np.float32, row_step=1, row_offset=0, out=None):
+    """row_step > 1 blends only the tile rows ty with ty % row_step ==
+    row_offset (a timing sample); `out` = (colors, alphas, last_ids) to write
+    into instead of new zeroed arrays (rows not blended are left as they are)."""
     means2d, conics, colors = _c(means2d, dtype), _c(conics, dtype), _c(colors, dtype)
     opacities, betas = _c(opacities, dtype), _c(betas, dtype)
     offs = _c(isect_offsets, np.int32)
@@ -226,20 +228,25 @@ def rasterize_to_pixels(means2d, conics, colors, opacities, betas, width, height
     mk = None if masks is None else _c(masks, np.uint8)
     C, th, tw = offs.shape
     N, cd = colors.shape[1], colors.shape[2]
-    oc = np.zeros((C, height, width, cd), dtype)
-    oa = np.zeros((C, height, width, 1), dtype)
-    li = np.zeros((C, height, width), np.int32)
+    if out is None:
+        oc = np.zeros((C, height, width, cd), dtype)
+        oa = np.zeros((C, height, width, 1), dtype)
+        li = np.zeros((C, height, width), np.int32)
+    else:
+        oc, oa, li = out
     _fn("raster_fwd", dtype)(C, N, cd, len(fl), _p(means2d), _p(conics), _p(colors),
                              _p(opacities), _p(betas), _p(bg), _p(mk), int(width), int(height),
                              int(tile_size), tw, th, _p(offs), _p(fl), _p(oc), _p(oa), _p(li),
-                             int(row_step))
+                             int(row_step) | (int(row_offset) << 16))
     return oc, oa, li
 
 
 def rasterize_to_pixels_bwd(means2d, conics, colors, opacities, betas, width, height,
                             tile_size, isect_offsets, flatten_ids, render_alphas, last_ids,
                             v_colors, v_alphas, backgrounds=None, masks=None, dtype=np.float32,
-                            row_step=1):
+                            row_step=1, row_offset=0, out=None):
+    """`out` = (v_means2d, v_conics, v_colors, v_opacities, v_betas) to add
+    into instead of new zeroed arrays."""
     means2d, conics, colors = _c(means2d, dtype), _c(conics, dtype), _c(colors, dtype)
     opacities, betas = _c(opacities, dtype), _c(betas, dtype)
     offs = _c(isect_offsets, np.int32)
@@ -250,13 +257,17 @@ def rasterize_to_pixels_bwd(means2d, conics, colors, opacities, betas, width, he
     vc, va = _c(v_colors, dtype), _c(v_alphas, dtype)
     C, th, tw = offs.shape
     N, cd = colors.shape[1], colors.shape[2]
-    vm2 = np.zeros((C, N, 2), dtype)
-    vcn = np.zeros((C, N, 3), dtype)
-    vcol = np.zeros((C, N, cd), dtype)
-    vo = np.zeros((C, N), dtype)
-    vb = np.zeros((C, N), dtype)
+    if out is None:
+        vm2 = np.zeros((C, N, 2), dtype)
+        vcn = np.zeros((C, N, 3), dtype)
+        vcol = np.zeros((C, N, cd), dtype)
+        vo = np.zeros((C, N), dtype)
+        vb = np.zeros((C, N), dtype)
+    else:
+        vm2, vcn, vcol, vo, vb = out
     _fn("raster_bwd", dtype)(C, N, cd, len(fl), _p(means2d), _p(conics), _p(colors),
                              _p(opacities), _p(betas), _p(bg), _p(mk), int(width), int(height),
                              int(tile_size), tw, th, _p(offs), _p(fl), _p(ra), _p(li), _p(vc),
-                             _p(va), _p(vm2), _p(vcn), _p(vcol), _p(vo), _p(vb), int(row_step))
+                             _p(va), _p(vm2), _p(vcn), _p(vcol), _p(vo), _p(vb),
+                             int(row_step) | (int(row_offset) << 16))
     return vm2, vcn, vcol, vo, vb

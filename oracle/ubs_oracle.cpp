@@ -864,7 +864,8 @@ void offset_encode(int64_t n_isects, const int64_t *isect_ids, int C, uint32_t t
 
 // ------------------------------------------------------- a9: blend forward
 // Per tile, per pixel, front to back over the tile's sorted range
-// (row_step > 1 blends only every row_step-th tile row: a timing sample):
+// (row_sel = row_step | row_offset << 16 with row_step > 1 blends only the
+// tile rows ty with ty % row_step == row_offset: a timing sample):
 // rasterize_to_pixels_fwd.cu:17-191.  Beta kernel alpha = min(0.999,
 // o * (1 - sigma)^beta) for 0 <= sigma < 1, exclusive termination at T <= 1e-4.
 template <typename T>
@@ -880,7 +881,7 @@ void raster_fwd(int C, int64_t N, int cdim, int64_t n_isects, const T *means2d,
         const int c = (int)(bt / n_tiles);
         const int64_t tile = bt % n_tiles;
         const int ty = (int)(tile / tw), tx = (int)(tile % tw);
-        if (ty % row_step) continue;
+        if (ty % (row_step & 0xffff) != (row_step >> 16)) continue;
         const int32_t rs = offsets[bt];
         const int32_t re = (c == C - 1 && tile == n_tiles - 1) ? (int32_t)n_isects : offsets[bt + 1];
         std::vector<T> acc(cdim);
@@ -942,7 +943,7 @@ void raster_bwd(int C, int64_t N, int cdim, int64_t n_isects, const T *means2d,
         const int c = (int)(bt / n_tiles);
         const int64_t tile = bt % n_tiles;
         const int ty = (int)(tile / tw), tx = (int)(tile % tw);
-        if (ty % row_step) continue;
+        if (ty % (row_step & 0xffff) != (row_step >> 16)) continue;
         const int32_t rs = offsets[bt];
         const int32_t re = (c == C - 1 && tile == n_tiles - 1) ? (int32_t)n_isects : offsets[bt + 1];
         std::vector<T> buf(cdim), vrc(cdim);
