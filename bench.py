@@ -64,6 +64,8 @@ def parse():
                          "for an ncu capture; prints no JSON line")
     ap.add_argument("--eager", action="store_true",
                     help="with --profile: launch the step kernel by kernel instead of a graph")
+    ap.add_argument("--dropin", action="store_true",
+                    help="with --profile: the step through the drop-in gsplat operators")
     return ap.parse_args()
 
 
@@ -648,6 +650,12 @@ def main():
     L.lib()
     p, cam, ri, rj, bg, target = make_problem(args.n_prims, rank, dev)
     fz = FusedStep(p, cam, bg, target, dev)
+    if args.profile and args.dropin:
+        for _ in range(args.warmup + 1):
+            gpu_step(p, cam, ri, rj, bg, target)
+        torch.cuda.synchronize()
+        print("profile run (drop-in operators)", flush=True)
+        return
     if args.profile and args.eager:
         fz.prime()
         for _ in range(args.warmup + 1):

@@ -546,6 +546,9 @@ int ubs_scene_forward(int32_t dim, int64_t N, const float *xyz, const float *mea
     UBS_REQUIRE(n_buckets >= 1 && capacity >= 1 && pix_base && render_colors && render_alphas &&
                     last_ids,
                 "scene_forward: bad buckets / capacity / outputs");
+    // bucket offsets are int32: one call holds fewer than 2^31 intersections
+    UBS_REQUIRE(capacity < (1ll << 31), "scene_forward: capacity %lld exceeds 2^31 - 1 "
+                "intersections; render fewer views per call", (long long)capacity);
     UBS_REQUIRE(workspace && ((uintptr_t)workspace & 255) == 0,
                 "scene_forward: workspace must be 256-byte aligned");
     const SceneWs w = scene_ws(workspace, C, N, n_buckets, capacity);
@@ -633,6 +636,8 @@ int ubs_scene_backward(int32_t dim, int64_t N, const float *xyz, const float *me
                     v_render_colors && v_render_alphas && v_xyz && v_mean && v_scale &&
                     v_l_triangle && v_opacity && v_beta && v_rgb,
                 "scene_backward: null argument");
+    UBS_REQUIRE(capacity < (1ll << 31), "scene_backward: capacity %lld exceeds 2^31 - 1",
+                (long long)capacity);
     UBS_REQUIRE(workspace && ((uintptr_t)workspace & 255) == 0,
                 "scene_backward: workspace must be 256-byte aligned");
     const SceneWs w = scene_ws(workspace, C, N, n_buckets, capacity);
