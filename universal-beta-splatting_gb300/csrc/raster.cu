@@ -457,28 +457,33 @@ __global__ void __launch_bounds__(512) raster_fwd_kernel(RasterArgs a) {
 // sum_k (c_k T - buf_k ra) v_k + T_final ra (v_a - bg.v); only the scalar
 // S = sum_k buf_k v_k enters, so it is carried instead of buf, and
 // K = T_final (v_a - bg.v) is folded once per pixel.
-template <int CD> struct BwdPix {
-    float T, S, K;
-    float vrc[CD];
-    int32_t bin;
-    bool inside;
+template <int CD> struct BwdPair {
+    float2 T, S, K;
+    float2 vrc[CD];
+    int32_t bin0, bin1;
+    bool in0, in1;
 };
 
 template <int CD>
-__device__ __forceinline__ void bwd_pix_init(BwdPix<CD> &s, const RasterArgs &a, int64_t pix,
-                                             bool inside, const float *bg) {
-    s.inside = inside;
-    const float T_final = 1.0f - a.render_alphas[pix];
-    s.T = T_final;
-    s.bin = inside ? a.last_in[pix] : 0;
-    float bgdot = 0.f;
+__device__ __forceinline__ void bwd_pair_init(BwdPair<CD> &s, const RasterArgs &a, int64_t pix0,
+                                              int64_t pix1, bool in0, bool in1, const float *bg) {
+    s.in0 = in0;
+    s.in1 = in1;
+    const float T0 = 1.0f - a.render_alphas[pix0], T1 = 1.0f - a.render_alphas[pix1];
+    s.T = make_float2(T0, T1);
+    s.bin0 = in0 ? a.last_in[pix0] : 0;
+    s.bin1 = in1 ? a.last_in[pix1] : 0;
+    float bg0 = 0.f, bg1 = 0.f;
 #pragma unroll
     for (int k = 0; k < CD; ++k) {
-        s.vrc[k] = a.v_out_c[pix * CD + k];
-        if (bg) bgdot += bg[k] * s.vrc[k];
+        s.vrc[k] = make_float2(a.v_out_c[pix0 * CD + k], a.v_out_c[pix1 * CD + k]);
+        if (bg) {
+            bg0 += bg[k] * s.vrc[k].x;
+            bg1 += bg[k] * s.vrc[k].y;
+        }
     }
-    s.K = T_final * (a.v_out_a[pix] - bgdot);
-    s.S = 0.f;
+    s.K = make_float2(T0 * (a.v_out_a[pix0] - bg0), T1 * (a.v_out_a[pix1] - bg1));
+    s.S = make_float2(0.f, 0.f);
 }
 
 // One back-to-front step of both pixels of a thread against record q
@@ -495,8 +500,8 @@ __device__ __forceinline__ void bwd_pix_init(BwdPix<CD> &s, const RasterArgs &a,
 // the flush (the conic, -opacity beta and opacity ln 2 factors).
 template <int CD>
 __device__ __forceinline__ bool grad_pair(const GeoRec &q, const float (&col)[CD], float px,
-                                          float2 npy, int32_t idx, BwdPix<CD> &s0,
-                                          BwdPix<CD> &s1, float (&g)[7 + CD]) {
+                                          float2 npy, int32_t idx, BwdPair<CD> &s,
+                                          float (&g)[7 + CD]) {
     const float dx = q.x - px;
     const float2 dy = __fadd2_rn(make_float2(q.y, q.y), npy);
     const float A = q.cxx * dx * dx;
@@ -504,8 +509,8 @@ __device__ __forceinline__ bool grad_pair(const GeoRec &q, const float (&col)[CD
     float2 sg = __fmul2_rn(make_float2(q.cyy, q.cyy), dy);
     sg = __ffma2_rn(sg, dy, make_float2(A, A));
     sg = __ffma2_rn(make_float2(B, B), dy, sg);
-    const bool v0 = s0.inside && idx <= s0.bin && !(sg.x < 0.f || sg.x >= 1.f);
-    const bool v1 = s1.inside && idx <= s1.bin && !(sg.y < 0.f || sg.y >= 1.f);
+    const bool v0 = s.in0 && idx <= s.bin0 && !(sg.x < 0.f || sg.x >= 1.f);
+    const bool v1 = s.in1 && idx <= s.bin1 && !(sg.y < 0.f || sg.y >= 1.f);
     if (!__any_sync(0xffffffffu, v0 || v1)) return false;
     float2 om = __ffma2_rn(sg, make_float2(-1.f, -1.f), make_float2(1.f, 1.f));
     om.x = v0 ? om.x : 1.f;
@@ -517,20 +522,20 @@ __device__ __forceinline__ bool grad_pair(const GeoRec &q, const float (&col)[CD
     const float2 alpha = make_float2(fminf(0.999f, ov.x), fminf(0.999f, ov.y));
     const float2 oma = __ffma2_rn(alpha, make_float2(-1.f, -1.f), make_float2(1.f, 1.f));
     const float2 ra = make_float2(1.0f / oma.x, 1.0f / oma.y);
-    const float2 Tn = __fmul2_rn(make_float2(s0.T, s1.T), ra);
+    const float2 Tn = __fmul2_rn(s.T, ra);
     float2 fac = __fmul2_rn(alpha, Tn);
     fac.x = v0 ? fac.x : 0.f;
     fac.y = v1 ? fac.y : 0.f;
-    float2 cv = __fmul2_rn(make_float2(col[0], col[0]), make_float2(s0.vrc[0], s1.vrc[0]));
+    float2 cv = __fmul2_rn(make_float2(col[0], col[0]), s.vrc[0]);
 #pragma unroll
     for (int k = 1; k < CD; ++k)
-        cv = __ffma2_rn(make_float2(col[k], col[k]), make_float2(s0.vrc[k], s1.vrc[k]), cv);
+        cv = __ffma2_rn(make_float2(col[k], col[k]), s.vrc[k], cv);
 #pragma unroll
     for (int k = 0; k < CD; ++k) {
-        const float2 gc = __fmul2_rn(fac, make_float2(s0.vrc[k], s1.vrc[k]));
+        const float2 gc = __fmul2_rn(fac, s.vrc[k]);
         g[7 + k] = gc.x + gc.y;
     }
-    const float2 kms = __fadd2_rn(make_float2(s0.K, s1.K), make_float2(-s0.S, -s1.S));
+    const float2 kms = __ffma2_rn(s.S, make_float2(-1.f, -1.f), s.K);
     float2 va = __ffma2_rn(Tn, cv, __fmul2_rn(ra, kms));
     va.x = (v0 && ov.x <= 0.999f) ? va.x : 0.f;
     va.y = (v1 && ov.y <= 0.999f) ? va.y : 0.f;
@@ -547,11 +552,9 @@ __device__ __forceinline__ bool grad_pair(const GeoRec &q, const float (&col)[CD
     g[4] = wdy2.x + wdy2.y;
     g[5] = u.x + u.y;
     g[6] = ul.x + ul.y;
-    const float2 S = __ffma2_rn(fac, cv, make_float2(s0.S, s1.S));
-    s0.S = S.x;
-    s1.S = S.y;
-    s0.T = v0 ? Tn.x : s0.T;
-    s1.T = v1 ? Tn.y : s1.T;
+    s.S = __ffma2_rn(fac, cv, s.S);
+    s.T.x = v0 ? Tn.x : s.T.x;
+    s.T.y = v1 ? Tn.y : s.T.y;
     return true;
 }
 
@@ -626,12 +629,11 @@ __global__ void __launch_bounds__(512) raster_bwd_kernel(RasterArgs a) {
 
     const float px = (float)j + 0.5f, py0 = (float)i0 + 0.5f, py1 = py0 + 1.f;
     const float2 npy = make_float2(-py0, -py1);
-    BwdPix<CD> s0, s1;
-    bwd_pix_init<CD>(s0, a, pix0, in0, bg);
-    bwd_pix_init<CD>(s1, a, pix1, in1, bg);
+    BwdPair<CD> sp;
+    bwd_pair_init<CD>(sp, a, pix0, pix1, in0, in1, bg);
 
     const int32_t wb = __reduce_max_sync(
-        0xffffffffu, max(in0 ? s0.bin : INT32_MIN, in1 ? s1.bin : INT32_MIN));
+        0xffffffffu, max(in0 ? sp.bin0 : INT32_MIN, in1 ? sp.bin1 : INT32_MIN));
     if (lane == 0) wbin[warp] = wb;
     for (int t = tid; t < BR * NV; t += NT) gacc[t] = 0.f;
     for (int t = tid; t < BR; t += NT) touched[t] = 0;
@@ -706,7 +708,7 @@ __global__ void __launch_bounds__(512) raster_bwd_kernel(RasterArgs a) {
                 float col[CD];
                 load_color<CD, PACK>(scol4, scol, buf * BR + t, col);
                 float g[NV];
-                if (!grad_pair<CD>(q, col, px, npy, idx, s0, s1, g)) continue;
+                if (!grad_pair<CD>(q, col, px, npy, idx, sp, g)) continue;
                 ReduceChunks<0, NV>::run(g, lane, gacc + t * NV);
                 if (lane == 0) touched[t] = 1;
             }
