@@ -44,6 +44,9 @@ N_PRIMS, DIM, WIDTH, HEIGHT, FOCAL, TILE = 1_000_000, 6, 1920, 1080, 1500.0, 16
 # rasterize_to_pixels_bwd.cu:170-247); rejected pairs are not counted.
 FWD_FLOP_PER_PAIR = 28
 BWD_FLOP_PER_PAIR = 77
+# learning rates of the reference's parameter groups (scene/beta_model.py:239-276)
+TRAIN_LRS = {"xyz": 1.6e-4, "mean": 2e-3, "rgb": 2.5e-3, "opacity": 5e-2, "beta": 5e-3,
+             "scale": 5e-3, "l_triangle": 1e-3}
 WORKLOAD = ("1M 6-D Beta primitives, 1920x1080 (fx=fy=1500), radius-4 orbit camera, 16x16 tiles; "
             "forward + L1 loss + backward to all raw parameters, one view per step")
 
@@ -733,8 +736,49 @@ def main():
     fwd_ms = time_steps(fz.forward, max(5, min(args.steps, 20)), dev, flush)
     fz.renderer._check_pending()
 
-    # the drop-in operator sequence (gsplat.rendering.rasterization call path)
     K2 = max(5, min(args.steps, 20))
+    # a full training iteration: the step plus the Adam update of the seven
+    # parameter groups, on a copy of the parameters (they change every step)
+    train_iter = None
+    try:
+        from ubs.optim import FusedAdam
+        from ubs.render import GraphedStep as _GS, Renderer as _R
+        p2 = {k: torch.nn.Parameter(v.detach().clone()) for k, v in p.items()}
+        groups2 = [{"params": [p2[k]], "lr": lr, "name": k} for k, lr in TRAIN_LRS.items()]
+        g_t2 = fz.target.clone()
+        gs2 = _GS(_R(dim=DIM, tile_size=TILE), p2, fz.views, fz.bg,
+                  lambda c, a: (c - g_t2).abs().mean(),
+                  optimizer=FusedAdam(groups2, lr=0.0, eps=1e-15))
+        for _ in range(3):
+            gs2.replay()
+        it_ms = time_steps(gs2.replay, K2, dev, flush)
+        gs2.check()
+        p3 = {k: torch.nn.Parameter(v.detach().clone()) for k, v in p.items()}
+        groups3 = [{"params": [p3[k]], "lr": lr, "name": k} for k, lr in TRAIN_LRS.items()]
+        adam3 = torch.optim.Adam(groups3, lr=0.0, eps=1e-15)
+        fz3 = FusedStep(p3, cam, bg, target, dev)
+        fz3.prime()
+
+        def torch_adam_iter():
+            fz3.step()
+            adam3.step()
+
+        for _ in range(3):
+            torch_adam_iter()
+        it3_ms = time_steps(torch_adam_iter, K2, dev, flush)
+        fz3.renderer._check_pending()
+        train_iter = {"value": 1000.0 / it_ms, "unit": "it/s", "ms_per_step": it_ms,
+                      "what": "render + L1 + backward + Adam update of the 7 parameter groups "
+                              "(FusedAdam, one kernel) as one CUDA graph",
+                      "with_torch_adam": {"value": 1000.0 / it3_ms, "ms_per_step": it3_ms,
+                                          "what": "the fused step launched kernel by kernel, "
+                                                  "then torch.optim.Adam (the reference's "
+                                                  "optimizer)"}}
+        del gs2, p2, p3, fz3, adam3
+    except Exception as e:  # noqa: BLE001
+        train_iter = {"error": repr(e)[:300]}
+
+    # the drop-in operator sequence (gsplat.rendering.rasterization call path)
     d_step = lambda: gpu_step(p, cam, ri, rj, bg, target)  # noqa: E731
     for _ in range(3):
         d_step()
@@ -849,6 +893,7 @@ def main():
             "roofline": roofline,
             "cpu_baseline": cpu,
             "ref_gpu": ref_gpu,
+            "train_iteration": train_iter,
             "eager": {"value": 1000.0 / eager_ms, "unit": "it/s", "ms_per_step": eager_ms,
                       "what": "the same fused step launched kernel by kernel (no graph)"},
             "dropin": {"value": 1000.0 / d_ms, "unit": "it/s", "ms_per_step": d_ms,

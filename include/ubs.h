@@ -227,6 +227,26 @@ int ubs_raster_bwd_packed(int32_t C, int64_t N, int32_t channels, int64_t n_isec
                           float *v_betas, int32_t zero_outputs, void *workspace,
                           size_t workspace_bytes, void *stream);
 
+/* ------------------------------------------------------------ optimizer ---
+ * One-launch Adam step over a scene's parameter tensors, the update of
+ * torch.optim.Adam(groups, eps) as the reference trains with it
+ * (scene/beta_model.py:239-276, train.py:170-171): per element
+ *   m = m + (1 - beta1) (g - m);  v = v beta2 + (1 - beta2) g g;
+ *   p = p + step_size m / (sqrt(v) / bc2 + eps)
+ * with step_size = -lr / (1 - beta1^t) and bc2 = sqrt(1 - beta2^t) read from
+ * device_hyper[2 * group], [2 * group + 1] (float, on the device, so that a
+ * captured launch follows the host's per-step updates of that array).
+ * 1 - beta1 and 1 - beta2 are passed as the caller rounds them (torch forms
+ * them in double before rounding to float).
+ * The table (device memory, ubs_adam_table_bytes) lists the tensors; fill a
+ * host copy with ubs_adam_table_entry and copy it to the device. */
+size_t ubs_adam_table_bytes(int32_t n_tensors);
+int ubs_adam_table_entry(void *host_table, int32_t index, float *param, const float *grad,
+                         float *exp_avg, float *exp_avg_sq, int64_t numel, int32_t group);
+int ubs_adam_step(int32_t n_tensors, const void *device_table, const float *device_hyper,
+                  int64_t max_numel, float one_minus_beta1, float beta2, float one_minus_beta2,
+                  float eps, void *stream);
+
 /* Forward blend without a workspace (no counterpart in the reference).
  * Same arguments, results and errors as ubs_raster_fwd minus the workspace,
  * for callers that cannot allocate device memory where they render (a host

@@ -68,6 +68,9 @@ SIGNATURES = {
     "ubs_profile_sample": ([], _INT),
     "ubs_profile_result": ([_I32, ctypes.POINTER(ctypes.c_char_p), _I64P,
                             ctypes.POINTER(ctypes.c_double)], _INT),
+    "ubs_adam_table_bytes": ([_I32], _SZ),
+    "ubs_adam_table_entry": ([_P, _I32, _P, _P, _P, _P, _I64, _I32], _INT),
+    "ubs_adam_step": ([_I32, _P, _P, _I64, _F, _F, _F, _F, _P], _INT),
     "ubs_fp32_probe_workspace_bytes": ([], _SZ),
     "ubs_fp32_probe": ([_I32, _P, _SZ, ctypes.POINTER(ctypes.c_double), _P], _INT),
 }

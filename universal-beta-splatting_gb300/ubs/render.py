@@ -279,11 +279,16 @@ class GraphedStep:
     the step must be captured again.  Capture on parameter tensors that have
     not been through an eager backward on the default stream (or on fresh
     copies of them): PyTorch's gradient accumulation for such leaves would
-    make the capture wait on that stream, which capture does not allow."""
+    make the capture wait on that stream, which capture does not allow.
+
+    With `optimizer` (ubs.optim.FusedAdam) the optimizer's update is captured
+    too: the gradients then keep fixed storage (allocated while warming up,
+    zeroed inside the graph) and `replay()` runs the optimizer's host part
+    (`prepare()`) before launching the graph."""
 
     def __init__(self, renderer: Renderer, params: Dict[str, torch.Tensor], views: Views,
                  backgrounds: Optional[torch.Tensor], loss_fn, headroom: float = 1.5,
-                 warmup: int = 3, before_capture=None):
+                 warmup: int = 3, before_capture=None, optimizer=None):
         self.r, self.p, self.views, self.loss_fn = renderer, params, views, loss_fn
         dev = params["xyz"].device
         self.bg = (torch.zeros(views.C, 3, device=dev) if backgrounds is None
@@ -291,6 +296,7 @@ class GraphedStep:
         with torch.no_grad():
             renderer.render(params, views, self.bg, check=True)
         renderer.capacity = int(renderer.last_isects * headroom) + 4096
+        self.optimizer = optimizer
         side = torch.cuda.Stream(dev)
         side.wait_stream(torch.cuda.current_stream(dev))
         with torch.cuda.stream(side):
@@ -298,15 +304,23 @@ class GraphedStep:
                 for v in params.values():
                     v.grad = None
                 self._body()
+                if optimizer is not None:
+                    optimizer.step()
         torch.cuda.current_stream(dev).wait_stream(side)
-        for v in params.values():
-            v.grad = None
+        if optimizer is None:
+            for v in params.values():
+                v.grad = None
         if before_capture is not None:
             before_capture()
         self.graph = torch.cuda.CUDAGraph()
         n0 = L.query("ubs_launch_count")
         with torch.cuda.graph(self.graph):
+            if optimizer is not None:
+                for v in params.values():
+                    v.grad.zero_()
             self.loss = self._body()
+            if optimizer is not None:
+                optimizer.launch()
         # library kernels in the graph (each replay launches them all)
         self.launches_per_replay = int(L.query("ubs_launch_count") - n0)
 
@@ -317,6 +331,8 @@ class GraphedStep:
         return loss
 
     def replay(self):
+        if self.optimizer is not None:
+            self.optimizer.prepare()
         self.graph.replay()
         return self.loss
 
