@@ -44,6 +44,13 @@ N_PRIMS, DIM, WIDTH, HEIGHT, FOCAL, TILE = 1_000_000, 6, 1920, 1080, 1500.0, 16
 # rasterize_to_pixels_bwd.cu:170-247); rejected pairs are not counted.
 FWD_FLOP_PER_PAIR = 28
 BWD_FLOP_PER_PAIR = 77
+# FP32 operations per (pixel, channel) of the SSIM training loss and its
+# gradient: two 11-tap passes (2 ops a tap) for the five windowed moments and
+# for the three derivative maps, plus ~40 for the products, the map, its
+# derivatives and the combine (utils/loss_utils.py:56-80, train.py:117-121)
+LOSS_FLOP_PER_PX = 2 * 11 * (5 * 2 + 3 * 2) + 40
+LOSS_BYTES_PER_PX = 12  # read the image and the target, write the gradient
+LAMBDA_DSSIM = 0.2      # arguments/__init__.py
 # learning rates of the reference's parameter groups (scene/beta_model.py:239-276)
 TRAIN_LRS = {"xyz": 1.6e-4, "mean": 2e-3, "rgb": 2.5e-3, "opacity": 5e-2, "beta": 5e-3,
              "scale": 5e-3, "l_triangle": 1e-3}
@@ -179,17 +186,48 @@ def gpu_step(p, cam, ri, rj, bg, target):
     return loss, meta
 
 
+_SSIM_WIN = {}
+
+
+def torch_l1_ssim(img, gt, lam=LAMBDA_DSSIM):
+    """train.py:117-121's loss on [N, 3, H, W] images with SSIM as
+    utils/loss_utils.py:26-80 formulates it in PyTorch (F.conv2d, 11 x 11
+    Gaussian window), the reference's own code for the SSIM term."""
+    import torch.nn.functional as F
+    c = img.shape[1]
+    key = (c, img.device)
+    if key not in _SSIM_WIN:
+        d = torch.arange(11, dtype=torch.float64) - 5
+        g = torch.exp(-d * d / (2 * 1.5 ** 2))
+        g = (g / g.sum()).float()
+        _SSIM_WIN[key] = (g[:, None] @ g[None, :]).expand(c, 1, 11, 11).contiguous().to(
+            img.device)
+    win = _SSIM_WIN[key]
+    conv = lambda a: F.conv2d(a, win, padding=5, groups=c)  # noqa: E731
+    mu1, mu2 = conv(img), conv(gt)
+    s1, s2 = conv(img * img) - mu1 ** 2, conv(gt * gt) - mu2 ** 2
+    s12 = conv(img * gt) - mu1 * mu2
+    C1, C2 = 0.01 ** 2, 0.03 ** 2
+    m = ((2 * mu1 * mu2 + C1) * (2 * s12 + C2)) / ((mu1 ** 2 + mu2 ** 2 + C1) * (s1 + s2 + C2))
+    return (1.0 - lam) * (img - gt).abs().mean() + lam * (1.0 - m.mean())
+
+
 class FusedStep:
     """One training step through the fused scene render: forward of the view,
-    L1 loss against the target, backward to all raw parameters."""
+    L1 loss against the target (or, with loss="l1_ssim_torch", the
+    reference's full training loss in PyTorch), backward to all raw
+    parameters."""
 
-    def __init__(self, p, cam, bg, target, dev):
+    def __init__(self, p, cam, bg, target, dev, loss="l1"):
         from ubs.render import Renderer, Views
         self.p = p
         self.renderer = Renderer(dim=DIM, tile_size=TILE)
         self.views = Views([cam], tile_size=TILE, device=dev)
         self.bg = bg.reshape(1, 3).contiguous()
         self.target = target.permute(1, 2, 0).reshape(-1, 3).contiguous()
+        self.loss = loss
+        self.hw = (cam.height, cam.width)
+        self.target_nchw = target[None].contiguous()
 
     def prime(self):
         """First frame with a synchronous capacity check (sizes the buffers)."""
@@ -200,13 +238,72 @@ class FusedStep:
         for v in self.p.values():
             v.grad = None
         colors, _ = self.renderer.render(self.p, self.views, self.bg, check=False)
-        loss = (colors - self.target).abs().mean()
+        if self.loss == "l1":
+            loss = (colors - self.target).abs().mean()
+        else:
+            img = colors.view(1, self.hw[0], self.hw[1], 3).permute(0, 3, 1, 2)
+            loss = torch_l1_ssim(img, self.target_nchw)
         loss.backward()
         return loss
 
     def forward(self):
         with torch.no_grad():
             self.renderer.render(self.p, self.views, self.bg, check=False)
+
+
+def bench_loss(dev, flush, K):
+    """The training loss and its gradient on one rendered 1920x1080 RGB image
+    (the renderer's [1, H, W, 3] layout): the fused kernel against the
+    PyTorch formulation of utils/loss_utils.py, and the kernel's roofline."""
+    from ubs import _lib as L
+    from ubs.loss import l1_ssim_loss
+    g = torch.Generator().manual_seed(0)
+    gt = torch.rand(1, HEIGHT, WIDTH, 3, generator=g)
+    img = (gt + 0.05 * torch.randn(gt.shape, generator=g)).clamp(0, 1)
+    gt, img = gt.to(dev), img.to(dev).requires_grad_(True)
+
+    def ours():
+        img.grad = None
+        l1_ssim_loss(img, gt, LAMBDA_DSSIM, channels_last=True).backward()
+
+    def plain():
+        img.grad = None
+        torch_l1_ssim(img.permute(0, 3, 1, 2), gt.permute(0, 3, 1, 2)).backward()
+
+    for _ in range(3):
+        ours()
+        plain()
+    t_ours = time_steps(ours, K, dev, flush)
+    t_plain = time_steps(plain, K, dev, flush)
+    L.profile_start(8 * (K + 1))
+    for _ in range(K):
+        flush.fill_(1.0)
+        ours()
+    torch.cuda.synchronize()
+    prof = L.profile_stop()
+    n_k, t_k = prof.get("ssim_loss_grad", (0, 0.0))
+    k_ms = t_k / max(1, n_k)
+    px = HEIGHT * WIDTH * 3
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    fp32 = fp32_peak(dev)
+    tflops = px * LOSS_FLOP_PER_PX / (k_ms * 1e-3) / 1e12 if k_ms else None
+    gbs = px * LOSS_BYTES_PER_PX / (k_ms * 1e-3) / 1e9 if k_ms else None
+    return {"ms": t_ours, "kernel_ms": k_ms, "plain_pytorch_ms": t_plain,
+            "speedup": t_plain / t_ours,
+            "what": "0.8 L1 + 0.2 (1 - SSIM) and its backward on one 1920x1080x3 image: "
+                    "one fused kernel (ubs.loss.l1_ssim_loss) vs the PyTorch formulation of "
+                    "utils/loss_utils.py (F.conv2d, default cuDNN settings)",
+            "roofline": {"bound": "fp32", "achieved": tflops, "peak": fp32, "unit": "TFLOP/s",
+                         "frac": tflops / fp32 if (tflops and fp32) else None,
+                         "algorithmic_work": "%d FP32 ops x %d pixel-channels" % (
+                             LOSS_FLOP_PER_PX, px),
+                         "hbm_gbs": gbs, "hbm_frac": gbs / peaks["hbm_gbs"]
+                         if (gbs and peaks.get("hbm_gbs")) else None,
+                         "hbm_bytes": px * LOSS_BYTES_PER_PX}}
 
 
 def time_steps(fn, K, dev, flush, after=None):
@@ -741,13 +838,15 @@ def main():
     # parameter groups, on a copy of the parameters (they change every step)
     train_iter = None
     try:
+        from ubs.loss import l1_ssim_loss
         from ubs.optim import FusedAdam
         from ubs.render import GraphedStep as _GS, Renderer as _R
         p2 = {k: torch.nn.Parameter(v.detach().clone()) for k, v in p.items()}
         groups2 = [{"params": [p2[k]], "lr": lr, "name": k} for k, lr in TRAIN_LRS.items()]
-        g_t2 = fz.target.clone()
+        g_t2 = fz.target.clone().view(1, HEIGHT, WIDTH, 3)
         gs2 = _GS(_R(dim=DIM, tile_size=TILE), p2, fz.views, fz.bg,
-                  lambda c, a: (c - g_t2).abs().mean(),
+                  lambda c, a: l1_ssim_loss(c.view(1, HEIGHT, WIDTH, 3), g_t2, LAMBDA_DSSIM,
+                                            channels_last=True),
                   optimizer=FusedAdam(groups2, lr=0.0, eps=1e-15))
         for _ in range(3):
             gs2.replay()
@@ -756,7 +855,7 @@ def main():
         p3 = {k: torch.nn.Parameter(v.detach().clone()) for k, v in p.items()}
         groups3 = [{"params": [p3[k]], "lr": lr, "name": k} for k, lr in TRAIN_LRS.items()]
         adam3 = torch.optim.Adam(groups3, lr=0.0, eps=1e-15)
-        fz3 = FusedStep(p3, cam, bg, target, dev)
+        fz3 = FusedStep(p3, cam, bg, target, dev, loss="l1_ssim_torch")
         fz3.prime()
 
         def torch_adam_iter():
@@ -768,15 +867,24 @@ def main():
         it3_ms = time_steps(torch_adam_iter, K2, dev, flush)
         fz3.renderer._check_pending()
         train_iter = {"value": 1000.0 / it_ms, "unit": "it/s", "ms_per_step": it_ms,
-                      "what": "render + L1 + backward + Adam update of the 7 parameter groups "
-                              "(FusedAdam, one kernel) as one CUDA graph",
+                      "what": "render + the reference's training loss 0.8 L1 + 0.2 (1 - SSIM) "
+                              "(one fused loss kernel) + backward + Adam update of the 7 "
+                              "parameter groups (FusedAdam, one kernel), as one CUDA graph",
                       "with_torch_adam": {"value": 1000.0 / it3_ms, "ms_per_step": it3_ms,
-                                          "what": "the fused step launched kernel by kernel, "
-                                                  "then torch.optim.Adam (the reference's "
+                                          "what": "the fused render launched kernel by kernel, "
+                                                  "the loss with SSIM as utils/loss_utils.py "
+                                                  "formulates it in PyTorch, then "
+                                                  "torch.optim.Adam (the reference's "
                                                   "optimizer)"}}
         del gs2, p2, p3, fz3, adam3
     except Exception as e:  # noqa: BLE001
         train_iter = {"error": repr(e)[:300]}
+
+    loss_res = None
+    try:
+        loss_res = bench_loss(dev, flush, max(10, min(args.steps, 50)))
+    except Exception as e:  # noqa: BLE001
+        loss_res = {"error": repr(e)[:300]}
 
     # the drop-in operator sequence (gsplat.rendering.rasterization call path)
     d_step = lambda: gpu_step(p, cam, ri, rj, bg, target)  # noqa: E731
@@ -894,6 +1002,7 @@ def main():
             "cpu_baseline": cpu,
             "ref_gpu": ref_gpu,
             "train_iteration": train_iter,
+            "loss": loss_res,
             "eager": {"value": 1000.0 / eager_ms, "unit": "it/s", "ms_per_step": eager_ms,
                       "what": "the same fused step launched kernel by kernel (no graph)"},
             "dropin": {"value": 1000.0 / d_ms, "unit": "it/s", "ms_per_step": d_ms,

@@ -247,6 +247,32 @@ int ubs_adam_step(int32_t n_tensors, const void *device_table, const float *devi
                   int64_t max_numel, float one_minus_beta1, float beta2, float one_minus_beta2,
                   float eps, void *stream);
 
+/* ----------------------------------------------------------------- loss ---
+ * The training loss  weight_l1 * mean|img - gt| + weight_ssim * mean(SSIM map)
+ * + weight_const  over a batch of images, with its gradient w.r.t. img in the
+ * same launch.  SSIM as utils/loss_utils.py:26-80 defines it (11 x 11 Gaussian
+ * window, sigma 1.5, zero padding, C1 = 0.01^2, C2 = 0.03^2) and as the
+ * fused_ssim package evaluates it for train.py:117-121; valid_padding != 0
+ * averages the map only over points at least 5 pixels from every edge
+ * (fused_ssim's padding="valid").  The reference's loss is weight_l1 = 1 - l,
+ * weight_ssim = -l, weight_const = l with l = lambda_dssim; fused_ssim alone
+ * is (0, 1, 0).
+ * Layouts are free: element (image n, channel c, row y, column x) of img sits
+ * at img + n s[0] + c s[1] + y s[2] + x s[3] for its strides s (int64[4]);
+ * gt and grad likewise.  grad == NULL computes the loss only.
+ * out (device, float[3]) receives mean(map), mean|img - gt| and the loss.
+ * The workspace (ubs_ssim_workspace_bytes) must be zero before its first use;
+ * every call leaves it zero again, so it can be reused by calls ordered on one
+ * stream (and by a captured launch). */
+size_t ubs_ssim_workspace_bytes(int32_t n_images, int32_t channels, int32_t height,
+                                int32_t width);
+int ubs_ssim_loss(const float *img, const int64_t *img_strides, const float *gt,
+                  const int64_t *gt_strides, float *grad, const int64_t *grad_strides,
+                  int32_t n_images, int32_t channels, int32_t height, int32_t width,
+                  int32_t valid_padding, double weight_l1, double weight_ssim,
+                  double weight_const, float *out, void *workspace, size_t workspace_bytes,
+                  void *stream);
+
 /* Forward blend without a workspace (no counterpart in the reference).
  * Same arguments, results and errors as ubs_raster_fwd minus the workspace,
  * for callers that cannot allocate device memory where they render (a host

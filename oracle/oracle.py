@@ -271,3 +271,75 @@ def rasterize_to_pixels_bwd(means2d, conics, colors, opacities, betas, width, he
                              _p(va), _p(vm2), _p(vcn), _p(vcol), _p(vo), _p(vb),
                              int(row_step) | (int(row_offset) << 16))
     return vm2, vcn, vcol, vo, vb
+
+
+# ------------------------------------------------------------------- loss ---
+SSIM_RADIUS = 5
+SSIM_C1 = 0.01 ** 2
+SSIM_C2 = 0.03 ** 2
+
+
+def ssim_window():
+    """Normalised 11-tap Gaussian of sigma 1.5, FP64 (utils/loss_utils.py:26-42
+    builds the same window, rounded to float32, as an outer product)."""
+    d = np.arange(2 * SSIM_RADIUS + 1, dtype=np.float64) - SSIM_RADIUS
+    g = np.exp(-d * d / (2 * 1.5 ** 2))
+    return g / g.sum()
+
+
+def _corr(a, g, axis):
+    """Zero-padded 'same' correlation of `a` with the symmetric window `g`
+    along `axis` (F.conv2d with padding 5, utils/loss_utils.py:57-73)."""
+    a = np.moveaxis(a, axis, -1)
+    n = a.shape[-1]
+    pad = np.pad(a, [(0, 0)] * (a.ndim - 1) + [(SSIM_RADIUS, SSIM_RADIUS)])
+    out = np.zeros_like(a)
+    for t in range(len(g)):
+        out += g[t] * pad[..., t:t + n]
+    return np.moveaxis(out, -1, axis)
+
+
+def _blur(a, g):
+    return _corr(_corr(a, g, -1), g, -2)
+
+
+def ssim_loss(img, gt, padding="same", w_l1=0.0, w_ssim=1.0, w_const=0.0):
+    """FP64 restatement of the training loss  w_l1 mean|img - gt| +
+    w_ssim mean(SSIM map) + w_const  and its gradient w.r.t. img.
+
+    img, gt: [N, C, H, W].  The map is utils/loss_utils.py:56-80's: windowed
+    means, variances and covariance with zero padding, C1 = 0.01^2,
+    C2 = 0.03^2; "valid" averages it over the points >= 5 pixels from every
+    edge (the fused_ssim package's padding="valid"); train.py:117-121 forms the
+    reference's loss as (w_l1, w_ssim, w_const) = (1 - l, -l, l).
+    The gradient is the analytic chain rule through the five windowed moments
+    (checked against finite differences and the reference's autograd in the
+    tests).  Returns (mean map, mean |img - gt|, loss, d loss / d img)."""
+    x = np.asarray(img, np.float64)
+    y = np.asarray(gt, np.float64)
+    g = ssim_window()
+    mx, my = _blur(x, g), _blur(y, g)
+    exx, eyy, exy = _blur(x * x, g), _blur(y * y, g), _blur(x * y, g)
+    vx, vy, cxy = exx - mx * mx, eyy - my * my, exy - mx * my
+    A1, A2 = 2 * mx * my + SSIM_C1, 2 * cxy + SSIM_C2
+    B1, B2 = mx * mx + my * my + SSIM_C1, vx + vy + SSIM_C2
+    smap = A1 * A2 / (B1 * B2)
+    H, W = x.shape[-2:]
+    mask = np.ones(x.shape, bool)
+    if padding == "valid":
+        r = SSIM_RADIUS
+        mask[...] = False
+        mask[..., r:H - r, r:W - r] = True
+    elif padding != "same":
+        raise ValueError(padding)
+    ms = smap[mask].mean()
+    ml = np.abs(x - y).mean()
+    loss = w_l1 * ml + w_ssim * ms + w_const
+    # d map / d (mx, E[x^2], E[xy]) with the E[.] moments free
+    d0 = 2 * my * (A2 - A1) / (B1 * B2) - 2 * mx * smap * (1 / B1 - 1 / B2)
+    d1 = -smap / B2
+    d2 = 2 * A1 / (B1 * B2)
+    scale = w_ssim / mask.sum() * mask
+    grad = _blur(d0 * scale, g) + 2 * x * _blur(d1 * scale, g) + y * _blur(d2 * scale, g)
+    grad += w_l1 / x.size * np.sign(x - y)
+    return ms, ml, loss, grad

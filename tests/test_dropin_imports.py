@@ -18,3 +18,11 @@ def test_beta_model_imports_resolve():
     for name in gsplat.__all__:
         assert callable(getattr(gsplat, name)), name
     assert callable(rasterization) and callable(_l_triangle_to_rotmat)
+
+
+def test_training_loss_imports_resolve():
+    """train.py:17 and scene/__init__.py:26 import fused_ssim."""
+    from fused_ssim import fused_ssim
+    import inspect
+    params = list(inspect.signature(fused_ssim).parameters)
+    assert params == ["img1", "img2", "padding", "train"]

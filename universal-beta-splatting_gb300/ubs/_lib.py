@@ -15,6 +15,7 @@ _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
 _I64 = ctypes.c_int64
 _F = ctypes.c_float
+_D = ctypes.c_double
 _SZ = ctypes.c_size_t
 _U32P = ctypes.POINTER(ctypes.c_uint32)
 _I64P = ctypes.POINTER(ctypes.c_int64)
@@ -71,6 +72,9 @@ SIGNATURES = {
     "ubs_adam_table_bytes": ([_I32], _SZ),
     "ubs_adam_table_entry": ([_P, _I32, _P, _P, _P, _P, _I64, _I32], _INT),
     "ubs_adam_step": ([_I32, _P, _P, _I64, _F, _F, _F, _F, _P], _INT),
+    "ubs_ssim_workspace_bytes": ([_I32, _I32, _I32, _I32], _SZ),
+    "ubs_ssim_loss": ([_P, _P, _P, _P, _P, _P, _I32, _I32, _I32, _I32, _I32, _D, _D, _D, _P,
+                       _P, _SZ, _P], _INT),
     "ubs_fp32_probe_workspace_bytes": ([], _SZ),
     "ubs_fp32_probe": ([_I32, _P, _SZ, ctypes.POINTER(ctypes.c_double), _P], _INT),
 }
@@ -177,6 +181,13 @@ def ptr(t, dtype=None):
         raise ValueError("expected a contiguous tensor")
     if dtype is not None and t.dtype != dtype:
         raise TypeError("expected dtype %s, got %s" % (dtype, t.dtype))
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def strided_ptr(t):
+    """Device pointer of a CUDA tensor whose strides the callee is given."""
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor, got device %s" % t.device)
     return ctypes.c_void_p(t.data_ptr())
 
 
