@@ -306,6 +306,204 @@ def bench_loss(dev, flush, K):
                          "hbm_bytes": px * LOSS_BYTES_PER_PX}}
 
 
+def _torch_densify(m, cap_max, noise_factor):
+    """The reference's densification step in PyTorch operations, for timing:
+    relocation of dead primitives and addition of new ones
+    (scene/beta_model.py:553-658) and the position noise (train.py:160-171),
+    with the host synchronisations those operations imply (mask sum,
+    nonzero, multinomial)."""
+    names = ("xyz", "mean", "rgb", "opacity", "beta", "scale", "l_triangle")
+    eps = torch.finfo(torch.float32).eps
+    opt = m.optimizer
+
+    def split(o_src, ratio):
+        new = 1.0 - torch.pow(1.0 - o_src, 1.0 / (ratio + 1))
+        new = torch.clamp(new, min=0.005, max=1.0 - eps)
+        return torch.log(new / (1 - new))
+
+    def draw(probs, num):
+        pick = torch.multinomial(probs / (probs.sum() + eps), num, replacement=True)
+        return pick
+
+    with torch.no_grad():
+        op = torch.sigmoid(m._opacity)
+        dead = (op <= 0.005).squeeze(-1)
+        if dead.sum() > 0:
+            dead_idx = dead.nonzero(as_tuple=True)[0]
+            alive_idx = (~dead).nonzero(as_tuple=True)[0]
+            pick = alive_idx[draw(op[alive_idx, 0], dead_idx.shape[0])]
+            ratio = torch.bincount(pick)[pick]
+            new_op = split(op[pick, 0], ratio).unsqueeze(-1)
+            for k in names:
+                t = getattr(m, "_" + k)
+                t.index_copy_(0, dead_idx, new_op if k == "opacity" else t[pick])
+            m._opacity.index_copy_(0, pick, m._opacity.index_select(0, dead_idx))
+            for k in names:
+                st = opt.state[getattr(m, "_" + k)]
+                st["exp_avg"][pick] = 0
+                st["exp_avg_sq"][pick] = 0
+        n = m._opacity.shape[0]
+        n_add = max(0, min(cap_max, int(1.02 * n)) - n)
+        if n_add > 0:
+            op = torch.sigmoid(m._opacity)
+            pick = draw(op[:, 0], n_add)
+            ratio = torch.bincount(pick)[pick]
+            new_op = split(op[pick, 0], ratio).unsqueeze(-1)
+            new = {k: (new_op if k == "opacity" else getattr(m, "_" + k)[pick]) for k in names}
+            m._opacity[pick] = new_op
+            for group in opt.param_groups:
+                k = group["name"]
+                old = group["params"][0]
+                st = opt.state.pop(old)
+                st["exp_avg"] = torch.cat([st["exp_avg"], torch.zeros_like(new[k])])
+                st["exp_avg_sq"] = torch.cat([st["exp_avg_sq"], torch.zeros_like(new[k])])
+                st["exp_avg"][pick] = 0
+                st["exp_avg_sq"][pick] = 0
+                p = torch.nn.Parameter(torch.cat([old, new[k]]).requires_grad_(True))
+                group["params"][0] = p
+                opt.state[p] = st
+                setattr(m, "_" + k, p)
+        # position noise with the spatial covariance R diag(s^2) R^T
+        s3 = torch.nn.functional.softplus(m._scale[:, :3])
+        l = m._l_triangle[:, :3]
+        one = torch.ones_like(l[:, 0])
+        R = torch.stack([one, l[:, 0], l[:, 1], -l[:, 0], one, l[:, 2], -l[:, 1], -l[:, 2],
+                         one], -1).view(-1, 3, 3)
+        M = R * s3[:, None, :]
+        cov = M @ M.transpose(1, 2)
+        noise = torch.randn_like(m._xyz) * torch.pow(1 - torch.sigmoid(m._opacity), 100) \
+            * noise_factor
+        m._xyz.add_(torch.bmm(cov, noise.unsqueeze(-1)).squeeze(-1))
+
+
+def bench_densify(p, dev, reps=5):
+    """One MCMC densification step (relocate + add + position noise) on the
+    1M-primitive scene with 10% dead primitives and Adam state: the device
+    sequence (ubs.mcmc) against the PyTorch operations of the reference, wall
+    clock per call with the device drained on both sides (the reference's
+    operations synchronise in the middle)."""
+    import time
+    import types
+    from ubs import mcmc
+    names = ("xyz", "mean", "rgb", "opacity", "beta", "scale", "l_triangle")
+    src = {"xyz": p["xyz"], "mean": p["mean"], "rgb": p["rgb"], "opacity": p["opacity"],
+           "beta": p["beta"], "scale": p["scale"], "l_triangle": p["l_triangle"]}
+    g = torch.Generator(device="cpu").manual_seed(0)
+    dead_rows = torch.rand(src["opacity"].shape[0], generator=g) < 0.1
+
+    def fresh():
+        m = types.SimpleNamespace()
+        groups = []
+        for k in names:
+            t = src[k].detach().clone().reshape(src[k].shape[0], -1)
+            if k == "opacity":
+                t[dead_rows.to(t.device)] = -8.0
+            prm = torch.nn.Parameter(t)
+            setattr(m, "_" + k, prm)
+            groups.append({"params": [prm], "lr": 1e-3, "name": k})
+        m.optimizer = torch.optim.Adam(groups, lr=0.0, eps=1e-15)
+        for k in names:
+            prm = getattr(m, "_" + k)
+            st = m.optimizer.state[prm]
+            st["step"] = torch.tensor(1.0)
+            st["exp_avg"] = torch.zeros_like(prm)
+            st["exp_avg_sq"] = torch.zeros_like(prm)
+        torch.cuda.synchronize()
+        return m
+
+    cap = 10 ** 9
+    factor = 1.0 * 1.6e-4
+
+    def ours(m):
+        mcmc.relocate_gs(m)
+        mcmc.add_new_gs(m, cap)
+        mcmc.perturb_xyz(m, factor)
+
+    res = {}
+    for name, fn in (("ours", ours), ("pytorch", lambda m: _torch_densify(m, cap, factor))):
+        fn(fresh())  # warm-up
+        ts = []
+        for _ in range(reps):
+            m = fresh()
+            t0 = time.perf_counter()
+            fn(m)
+            torch.cuda.synchronize()
+            ts.append((time.perf_counter() - t0) * 1e3)
+            del m
+        res[name] = sorted(ts)[len(ts) // 2]
+    return {"ms": res["ours"], "plain_pytorch_ms": res["pytorch"],
+            "speedup": res["pytorch"] / res["ours"],
+            "what": "one MCMC densification step on 1M primitives with 10%% dead and Adam "
+                    "state: relocation, +2%% addition, position noise; device kernels "
+                    "(ubs.mcmc, no host synchronisation) vs the reference's PyTorch "
+                    "operations (scene/beta_model.py:553-658, train.py:160-171); median "
+                    "wall clock of %d calls" % reps}
+
+
+def bench_scene_file(p, dev, reps=3):
+    """Save and load of the 1M-primitive scene in the reference's PLY format:
+    this library (native header/body I/O, chunked pinned copies, one
+    pack/unpack kernel) against the reference's load_ply steps
+    (scene/beta_model.py:322-404: per-property gathers into float64 arrays,
+    then one torch.tensor(..., device="cuda") per parameter) with plyfile's
+    binary read replaced by numpy's structured read (plyfile is not installed
+    here).  The file sits in /tmp (page cache); median wall clock."""
+    import tempfile
+    import time
+    from ubs import ply
+    path = os.path.join(tempfile.gettempdir(), "ubs_bench_scene.ply")
+    names = ("xyz", "mean", "rgb", "opacity", "beta", "scale", "l_triangle")
+
+    def ref_load():
+        n, props, off = ply.read_header(path)
+        rec = np.fromfile(path, dtype=[(nm, "<f4") for nm in props], offset=off, count=n)
+
+        def fam(prefix):
+            sel = sorted([nm for nm in props if nm.startswith(prefix)],
+                         key=lambda s: int(s.split("_")[-1]))
+            out = np.zeros((n, len(sel)))
+            for i, nm in enumerate(sel):
+                out[:, i] = np.asarray(rec[nm])
+            return out
+
+        xyz = np.stack((np.asarray(rec["x"]), np.asarray(rec["y"]), np.asarray(rec["z"])), 1)
+        rgb = np.zeros((n, 3))
+        for i, nm in enumerate(("red", "green", "blue")):
+            rgb[:, i] = np.asarray(rec[nm])
+        arrays = {"xyz": xyz, "mean": fam("mean_"), "rgb": rgb,
+                  "opacity": np.asarray(rec["opacity"])[..., None], "beta": fam("beta_"),
+                  "scale": fam("scale_"), "l_triangle": fam("l_triangle")}
+        return {k: torch.tensor(arrays[k], dtype=torch.float, device=dev) for k in names}
+
+    def med(fn):
+        ts = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append((time.perf_counter() - t0) * 1e3)
+        return sorted(ts)[len(ts) // 2]
+
+    try:
+        save_ms = med(lambda: ply.save_ply(path, p))
+        load_ms = med(lambda: ply.load_ply(path, dev))
+        ref_ms = med(ref_load)
+        q = ply.load_ply(path, dev)
+        r = ref_load()
+        same = all(torch.equal(q[k], r[k]) for k in names)
+        size = os.path.getsize(path)
+    finally:
+        if os.path.exists(path):
+            os.remove(path)
+    return {"save_ms": save_ms, "load_ms": load_ms, "reference_steps_load_ms": ref_ms,
+            "load_speedup": ref_ms / load_ms, "file_bytes": size, "identical": same,
+            "load_gbs": size / (load_ms * 1e-3) / 1e9,
+            "what": "1M-primitive 6-D scene file (reference PLY layout): save and load "
+                    "through ubs.ply vs the reference's load_ply steps with numpy's "
+                    "structured read standing in for plyfile; median of %d" % reps}
+
+
 def time_steps(fn, K, dev, flush, after=None):
     """Per-step CUDA-event time (ms), L2 flushed before every step (untimed);
     `after` runs after each step, outside the timed events."""
@@ -885,6 +1083,17 @@ def main():
         loss_res = bench_loss(dev, flush, max(10, min(args.steps, 50)))
     except Exception as e:  # noqa: BLE001
         loss_res = {"error": repr(e)[:300]}
+    densify = None
+    try:
+        densify = bench_densify(p, dev)
+    except Exception as e:  # noqa: BLE001
+        densify = {"error": repr(e)[:300]}
+    torch.cuda.empty_cache()
+    scene_file = None
+    try:
+        scene_file = bench_scene_file(p, dev)
+    except Exception as e:  # noqa: BLE001
+        scene_file = {"error": repr(e)[:300]}
 
     # the drop-in operator sequence (gsplat.rendering.rasterization call path)
     d_step = lambda: gpu_step(p, cam, ri, rj, bg, target)  # noqa: E731
@@ -1003,6 +1212,8 @@ def main():
             "ref_gpu": ref_gpu,
             "train_iteration": train_iter,
             "loss": loss_res,
+            "densify": densify,
+            "scene_file": scene_file,
             "eager": {"value": 1000.0 / eager_ms, "unit": "it/s", "ms_per_step": eager_ms,
                       "what": "the same fused step launched kernel by kernel (no graph)"},
             "dropin": {"value": 1000.0 / d_ms, "unit": "it/s", "ms_per_step": d_ms,

@@ -273,6 +273,91 @@ int ubs_ssim_loss(const float *img, const int64_t *img_strides, const float *gt,
                   double weight_const, float *out, void *workspace, size_t workspace_bytes,
                   void *stream);
 
+/* --------------------------------------------------- MCMC densification ---
+ * BetaModel.relocate_gs / add_new_gs (scene/beta_model.py:553-658) and the
+ * position noise of train.py:164-171, on the device with no host
+ * synchronisation (sizes never depend on the data, so the calls can be
+ * captured in a CUDA graph).
+ * A scene is a set of per-primitive FP32 tensors [n, width[k]] (the
+ * reference's seven: xyz, mean, rgb, opacity, beta, scale, l_triangle) with
+ * their Adam moments (NULL where a tensor has no optimizer state yet). */
+#define UBS_MCMC_MAX_TENSORS 8
+typedef struct ubs_mcmc_tensors {
+    int32_t n_tensors;     /* 1 .. UBS_MCMC_MAX_TENSORS                       */
+    int32_t opacity_index; /* the raw (pre-sigmoid) opacity, width 1           */
+    int32_t width[UBS_MCMC_MAX_TENSORS];
+    float *param[UBS_MCMC_MAX_TENSORS];
+    float *exp_avg[UBS_MCMC_MAX_TENSORS];
+    float *exp_avg_sq[UBS_MCMC_MAX_TENSORS];
+} ubs_mcmc_tensors;
+
+size_t ubs_mcmc_workspace_bytes(int64_t n_prims, int64_t n_draw_max);
+/* In place: every dead primitive (dead_mask[i] != 0, or, with a NULL mask,
+ * sigmoid(raw opacity) <= dead_threshold) becomes a copy of a live one drawn
+ * with probability proportional to its opacity; a primitive drawn c times and
+ * its c copies share logit(clamp(1 - (1 - o)^(1/(c+1)), 0.005, 1 - eps));
+ * the drawn primitives' Adam moments are zeroed.  Draws come from a counter-
+ * based generator keyed by `seed`, or from given_src (n_given live indices,
+ * one per dead primitive in index order) to reproduce other draws.  No live
+ * primitive: nothing changes.  Bad given indices set a bit in *status
+ * (device word, not cleared). */
+int ubs_mcmc_relocate(const ubs_mcmc_tensors *scene, int64_t n_prims, const uint8_t *dead_mask,
+                      float dead_threshold, uint64_t seed, const int64_t *given_src,
+                      int64_t n_given, uint32_t *status, void *workspace,
+                      size_t workspace_bytes, void *stream);
+/* Writes `grown` (tensors of n_prims + n_add rows, the scene's widths and
+ * moment layout): rows < n_prims copy the scene, drawn primitives with their
+ * split opacity and zero moments; row n_prims + j copies the j-th draw (from
+ * all primitives, proportional to opacity, or given_src[j]) with the split
+ * opacity and zero moments. */
+int ubs_mcmc_add(const ubs_mcmc_tensors *scene, const ubs_mcmc_tensors *grown, int64_t n_prims,
+                 int64_t n_add, uint64_t seed, const int64_t *given_src, uint32_t *status,
+                 void *workspace, size_t workspace_bytes, void *stream);
+/* xyz += Sigma_xyz (z (1 - sigmoid(raw_opacity))^100 factor) with z standard
+ * normal (given_noise [n, 3], or drawn from `seed`), Sigma_xyz = R diag(s^2)
+ * R^T, s = softplus(raw_scale[:, :3]) (row stride dim), R = I + A from
+ * l_triangle[:, :3] (row stride dim (dim - 1) / 2); factor = noise_lr * lr. */
+int ubs_mcmc_perturb_xyz(int64_t n_prims, int32_t dim, float *xyz, const float *raw_opacity,
+                         const float *raw_scale, const float *l_triangle, float factor,
+                         uint64_t seed, const float *given_noise, void *stream);
+
+/* ----------------------------------------------------------- scene files ---
+ * The reference's scene file (scene/beta_model.py:286-404): one PLY "vertex"
+ * element of float32 properties x, y, z, red, green, blue, opacity, beta_i,
+ * mean_i, scale_i, l_triangle_i, binary little-endian.
+ * ubs_ply_read_header parses a header (comments and obj_info lines allowed;
+ * other elements only if empty; vertex properties must all be float) and
+ * returns the vertex count, the property count, the property names (when
+ * `names` is given: UBS_PLY_NAME_BYTES bytes each, NUL-terminated, at most
+ * names_capacity of them) and the byte offset of the body; ascii or
+ * big-endian files return UBS_ERR_UNSUPPORTED.
+ * ubs_ply_read_body reads n_bytes of the body from `offset` into host memory
+ * (pinned memory lets the caller overlap the next read with the copy to the
+ * device).  ubs_ply_write writes a header with the given names and the
+ * records (n_vertices x n_props float32, host memory).
+ * ubs_ply_unpack scatters device records [n, record_floats] into the layout's
+ * tensors; ubs_ply_pack gathers them back (unmapped properties read 0). */
+#define UBS_PLY_MAX_TENSORS 8
+#define UBS_PLY_MAX_PROPS 256
+#define UBS_PLY_NAME_BYTES 64
+typedef struct ubs_ply_layout {
+    int32_t record_floats;                  /* properties per vertex           */
+    int32_t n_tensors;                      /* 0 .. UBS_PLY_MAX_TENSORS        */
+    int32_t width[UBS_PLY_MAX_TENSORS];     /* floats per primitive            */
+    float *param[UBS_PLY_MAX_TENSORS];      /* device tensors [n, width]       */
+    int16_t tensor_of[UBS_PLY_MAX_PROPS];   /* property -> tensor, -1: skipped */
+    int16_t column_of[UBS_PLY_MAX_PROPS];   /* property -> column in its tensor */
+} ubs_ply_layout;
+int ubs_ply_read_header(const char *path, int64_t *n_vertices, int32_t *n_props, char *names,
+                        int32_t names_capacity, int64_t *body_offset);
+int ubs_ply_read_body(const char *path, int64_t offset, void *dst, int64_t n_bytes);
+int ubs_ply_write(const char *path, int64_t n_vertices, int32_t n_props, const char *names,
+                  const void *records);
+int ubs_ply_unpack(const ubs_ply_layout *layout, const float *records, int64_t n_vertices,
+                   void *stream);
+int ubs_ply_pack(const ubs_ply_layout *layout, float *records, int64_t n_vertices,
+                 void *stream);
+
 /* Forward blend without a workspace (no counterpart in the reference).
  * Same arguments, results and errors as ubs_raster_fwd minus the workspace,
  * for callers that cannot allocate device memory where they render (a host

@@ -343,3 +343,172 @@ def ssim_loss(img, gt, padding="same", w_l1=0.0, w_ssim=1.0, w_const=0.0):
     grad = _blur(d0 * scale, g) + 2 * x * _blur(d1 * scale, g) + y * _blur(d2 * scale, g)
     grad += w_l1 / x.size * np.sign(x - y)
     return ms, ml, loss, grad
+
+
+# ------------------------------------------------------ MCMC densification ---
+MCMC_NAMES = ("xyz", "mean", "rgb", "opacity", "beta", "scale", "l_triangle")
+_F32_EPS = np.float32(np.finfo(np.float32).eps)
+
+
+def mcmc_split_opacity(raw_opacity, count):
+    """Raw opacity of a primitive sampled `count` times, shared by it and its
+    copies (scene/beta_model.py:553-562, FP32):
+    logit(clamp(1 - (1 - sigmoid(raw))^(1 / (count + 1)), 0.005, 1 - eps))."""
+    raw = np.asarray(raw_opacity, np.float32)
+    o = (np.float32(1) / (np.float32(1) + np.exp(-raw))).astype(np.float32)
+    e = (np.float32(1) / (np.asarray(count) + 1).astype(np.float32)).astype(np.float32)
+    new = (np.float32(1) - np.power(np.float32(1) - o, e)).astype(np.float32)
+    new = np.minimum(np.maximum(new, np.float32(0.005)), np.float32(1) - _F32_EPS)
+    return np.log(new / (np.float32(1) - new)).astype(np.float32)
+
+
+def mcmc_relocate(params, moments, dead, src):
+    """BetaModel.relocate_gs (scene/beta_model.py:585-621) given the sampled
+    live indices `src` (one per dead primitive, in index order): every dead
+    primitive becomes a copy of its source with the split opacity, the sources
+    take that opacity too, and the sources' Adam moments are zeroed (the dead
+    slots keep theirs, as in the reference).  params: name -> [N, c];
+    moments: name -> (exp_avg, exp_avg_sq).  Returns new dicts."""
+    dead_idx = np.nonzero(np.asarray(dead))[0]
+    src = np.asarray(src, np.int64)
+    out = {k: np.array(v, np.float32, copy=True) for k, v in params.items()}
+    mom = {k: (np.array(m, np.float32, copy=True), np.array(v, np.float32, copy=True))
+           for k, (m, v) in moments.items()}
+    if len(dead_idx) == 0 or len(src) == 0:
+        return out, mom
+    N = out["opacity"].shape[0]
+    count = np.bincount(src, minlength=N)
+    new_op = mcmc_split_opacity(out["opacity"][src, 0], count[src])
+    for k in params:
+        out[k][dead_idx] = params[k][src]
+    out["opacity"][dead_idx, 0] = new_op
+    out["opacity"][src] = out["opacity"][dead_idx]
+    for k, (m, v) in mom.items():
+        m[src] = 0
+        v[src] = 0
+    return out, mom
+
+
+def mcmc_add(params, moments, src):
+    """BetaModel.add_new_gs (scene/beta_model.py:623-658) given the sampled
+    indices `src` (one per new primitive): the new primitives, appended in
+    order, copy their sources with the split opacity; the sources take that
+    opacity; the grown Adam moments are zero for the new rows and at the
+    sources."""
+    src = np.asarray(src, np.int64)
+    N = params["opacity"].shape[0]
+    count = np.bincount(src, minlength=N)
+    new_op = mcmc_split_opacity(params["opacity"][src, 0], count[src])
+    new = {k: np.array(v, np.float32)[src] for k, v in params.items()}
+    new["opacity"][:, 0] = new_op
+    out = {k: np.array(v, np.float32, copy=True) for k, v in params.items()}
+    out["opacity"][src, 0] = new_op
+    out = {k: np.concatenate([out[k], new[k]], 0) for k in params}
+    mom = {}
+    for k, (m, v) in moments.items():
+        m2 = np.concatenate([m, np.zeros_like(new[k])], 0).astype(np.float32)
+        v2 = np.concatenate([v, np.zeros_like(new[k])], 0).astype(np.float32)
+        m2[src] = 0
+        v2[src] = 0
+        mom[k] = (m2, v2)
+    return out, mom
+
+
+def mcmc_add_count(n_prims, cap_max):
+    """Primitives add_new_gs appends (scene/beta_model.py:624-626)."""
+    return max(0, min(int(cap_max), int(1.02 * n_prims)) - int(n_prims))
+
+
+def xyz_covariance(raw_scale, l_triangle):
+    """Spatial 3 x 3 block of the primitive covariance (get_xyz_covariance,
+    scene/beta_model.py:144-152): R diag(s^2) R^T with s = softplus of the
+    first three raw scales and R = I + A from l_triangle[:, :3]."""
+    s = np.log1p(np.exp(np.asarray(raw_scale, np.float64)[:, :3]))
+    R = l_triangle_to_rotmat(np.asarray(l_triangle, np.float64)[:, :3], dtype=np.float64)
+    M = R * s[:, None, :]
+    return M @ np.transpose(M, (0, 2, 1))
+
+
+def mcmc_perturb_xyz(xyz, raw_opacity, raw_scale, l_triangle, noise, factor):
+    """train.py:164-171: xyz + Sigma_xyz (noise (1 - sigmoid(raw_opacity))^100
+    factor), factor = noise_lr * xyz_lr, for given standard-normal noise."""
+    o = 1.0 / (1.0 + np.exp(-np.asarray(raw_opacity, np.float64)))
+    n = np.asarray(noise, np.float64) * (1.0 - o) ** 100 * factor
+    cov = xyz_covariance(raw_scale, l_triangle)
+    return np.asarray(xyz, np.float64) + np.einsum("nij,nj->ni", cov, n)
+
+
+# ------------------------------------------------------------ scene files ---
+def ply_attribute_names(n_beta, n_mean, n_scale, n_ltri):
+    """construct_list_of_attributes (scene/beta_model.py:286-296)."""
+    return (["x", "y", "z", "red", "green", "blue", "opacity"]
+            + ["beta_%d" % i for i in range(n_beta)] + ["mean_%d" % i for i in range(n_mean)]
+            + ["scale_%d" % i for i in range(n_scale)]
+            + ["l_triangle_%d" % i for i in range(n_ltri)])
+
+
+def ply_bytes(params, names=None, comments=()):
+    """The bytes of the reference's scene file (save_ply, beta_model.py:298-320:
+    one vertex element, float32 properties, binary little-endian, written by
+    plyfile) for raw parameters {xyz, mean, rgb, opacity, beta, scale,
+    l_triangle}; `names` reorders or extends the properties (a name not in the
+    default list is written as zeros) and `comments` adds comment lines."""
+    cols = {}
+    p = {}
+    for k, v in params.items():
+        a = np.asarray(v, np.float32)
+        p[k] = a[:, None] if a.ndim == 1 else a.reshape(a.shape[0], -1 if a.shape[0] else
+                                                        int(np.prod(a.shape[1:])))
+    for i, c in enumerate("xyz"):
+        cols[c] = p["xyz"][:, i]
+    for i, c in enumerate(("red", "green", "blue")):
+        cols[c] = p["rgb"][:, i]
+    cols["opacity"] = p["opacity"][:, 0]
+    for fam, key in (("beta", "beta"), ("mean", "mean"), ("scale", "scale"),
+                     ("l_triangle", "l_triangle")):
+        for i in range(p[key].shape[1]):
+            cols["%s_%d" % (fam, i)] = p[key][:, i]
+    default = ply_attribute_names(p["beta"].shape[1], p["mean"].shape[1], p["scale"].shape[1],
+                                  p["l_triangle"].shape[1])
+    names = list(default if names is None else names)
+    n = p["xyz"].shape[0]
+    head = "ply\nformat binary_little_endian 1.0\n"
+    head += "".join("comment %s\n" % c for c in comments)
+    head += "element vertex %d\n" % n
+    head += "".join("property float %s\n" % nm for nm in names) + "end_header\n"
+    rec = np.zeros((n, len(names)), "<f4")
+    for j, nm in enumerate(names):
+        if nm in cols:
+            rec[:, j] = cols[nm]
+    return head.encode() + rec.tobytes()
+
+
+def ply_parse(data):
+    """Raw parameters read from scene-file bytes the way load_ply
+    (beta_model.py:322-404) reads them: by property name, each of the beta_,
+    mean_, scale_, l_triangle families sorted by numeric suffix."""
+    end = data.index(b"end_header\n") + len(b"end_header\n")
+    lines = data[:end].decode().splitlines()
+    assert lines[0] == "ply" and lines[1] == "format binary_little_endian 1.0"
+    n = None
+    names = []
+    for ln in lines[2:]:
+        w = ln.split()
+        if w[0] == "element" and w[1] == "vertex":
+            n = int(w[2])
+        elif w[0] == "property":
+            assert w[1] in ("float", "float32")
+            names.append(w[2])
+    rec = np.frombuffer(data[end:end + n * len(names) * 4], "<f4").reshape(n, len(names))
+    col = {nm: rec[:, i] for i, nm in enumerate(names)}
+
+    def fam(prefix):
+        sel = sorted([nm for nm in names if nm.startswith(prefix)],
+                     key=lambda s: int(s.split("_")[-1]))
+        return np.stack([col[s] for s in sel], 1) if sel else np.zeros((n, 0), np.float32)
+
+    return {"xyz": np.stack([col["x"], col["y"], col["z"]], 1),
+            "rgb": np.stack([col["red"], col["green"], col["blue"]], 1),
+            "opacity": col["opacity"][:, None].copy(),
+            "mean": fam("mean_"), "beta": fam("beta_"), "scale": fam("scale_"),
+            "l_triangle": fam("l_triangle")}

@@ -72,6 +72,16 @@ SIGNATURES = {
     "ubs_adam_table_bytes": ([_I32], _SZ),
     "ubs_adam_table_entry": ([_P, _I32, _P, _P, _P, _P, _I64, _I32], _INT),
     "ubs_adam_step": ([_I32, _P, _P, _I64, _F, _F, _F, _F, _P], _INT),
+    "ubs_ply_read_header": ([ctypes.c_char_p, _I64P, ctypes.POINTER(ctypes.c_int32), _P, _I32,
+                             _I64P], _INT),
+    "ubs_ply_read_body": ([ctypes.c_char_p, _I64, _P, _I64], _INT),
+    "ubs_ply_write": ([ctypes.c_char_p, _I64, _I32, _P, _P], _INT),
+    "ubs_ply_unpack": ([_P, _P, _I64, _P], _INT),
+    "ubs_ply_pack": ([_P, _P, _I64, _P], _INT),
+    "ubs_mcmc_workspace_bytes": ([_I64, _I64], _SZ),
+    "ubs_mcmc_relocate": ([_P, _I64, _P, _F, ctypes.c_uint64, _P, _I64, _P, _P, _SZ, _P], _INT),
+    "ubs_mcmc_add": ([_P, _P, _I64, _I64, ctypes.c_uint64, _P, _P, _P, _SZ, _P], _INT),
+    "ubs_mcmc_perturb_xyz": ([_I64, _I32, _P, _P, _P, _P, _F, ctypes.c_uint64, _P, _P], _INT),
     "ubs_ssim_workspace_bytes": ([_I32, _I32, _I32, _I32], _SZ),
     "ubs_ssim_loss": ([_P, _P, _P, _P, _P, _P, _I32, _I32, _I32, _I32, _I32, _D, _D, _D, _P,
                        _P, _SZ, _P], _INT),
