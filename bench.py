@@ -504,6 +504,85 @@ def bench_scene_file(p, dev, reps=3):
                     "structured read standing in for plyfile; median of %d" % reps}
 
 
+def bench_viewer(p, cam, dev, reps=10):
+    """Viewer frames of the 1M-primitive scene at 1920x1080 with Beta
+    quantile ranges (5-95 % spatial, 5-95 % view): ubs.viewer.FrameRenderer
+    against the steps of the reference's BetaModel.view
+    (scene/beta_model.py:725-831: torch.quantile masks, conditioning, masked
+    gathers, rasterization(), torch depth colormap, .cpu()) run on this
+    library's drop-in operators; wall clock per frame to a host array."""
+    import time
+    import torch.nn.functional as F
+    from gsplat.cuda._wrapper import (cond_mean_convariance_opacity, l_triangle_to_rotmat,
+                                      rot_scale_l_triangle_to_covar)
+    from gsplat.rendering import rasterization
+    from ubs import scene as S
+    from ubs.viewer import FrameRenderer, ViewState
+    c2w = torch.inverse(cam.viewmat.cpu()).numpy()
+    K = cam.K.cpu().numpy()
+    table = torch.rand(256, 3, generator=torch.Generator().manual_seed(0)).to(dev)
+    ri, rj = S.rest_indices(DIM, dev)
+
+    def steps(mode):
+        st = ViewState(b_xyz=(5, 95), b_view=(5, 95), render_mode=mode)
+        c2w_t = torch.from_numpy(c2w).float().to(dev)
+        K_t = torch.from_numpy(K).float().to(dev)
+        beta_raw = p["beta"]
+        x, v = beta_raw[:, 0], beta_raw[:, 1:4].mean(dim=-1)
+        mask = ((x >= x.quantile(0.05)) & (x <= x.quantile(0.95)) & (v >= v.quantile(0.05))
+                & (v <= v.quantile(0.95)))
+        vd = p["xyz"] - c2w_t[:3, 3][None]
+        q = vd / vd.norm(dim=-1, keepdim=True)
+        scale = F.softplus(p["scale"])
+        beta = 4.0 * torch.exp(p["beta"])
+        R = l_triangle_to_rotmat(p["l_triangle"][:, :3])
+        cov = rot_scale_l_triangle_to_covar(R, scale, p["l_triangle"], ri, rj)
+        means, convs, opac = cond_mean_convariance_opacity(
+            torch.cat([p["xyz"], p["mean"]], -1), cov, torch.sigmoid(p["opacity"]), beta[:, 1:],
+            q)
+        bg = torch.tensor(st.backgrounds, device=dev) / 255.0
+        rc, ra, meta = rasterization(
+            means=means[mask], l_triagnles=p["l_triangle"][mask], scales=scale[mask],
+            opacities=opac.squeeze()[mask], betas=beta[:, :1].squeeze()[mask],
+            colors=p["rgb"][mask], viewmats=torch.linalg.inv(c2w_t)[None], Ks=K_t[None],
+            width=WIDTH, height=HEIGHT, backgrounds=bg[None], render_mode=mode,
+            covars=convs[mask], near_plane=st.near_plane, far_plane=st.far_plane)
+        int((meta["radii"] > 0).sum().item())
+        if rc.shape[-1] == 1:
+            near, far = float(torch.min(rc)), float(torch.max(rc))
+            d = torch.nan_to_num(torch.clip((rc - near) / (far - near + 1e-10), 0.0, 1.0), 0)
+            rc = table[(d * 255).long()[..., 0]]
+        return rc[0].cpu().numpy()
+
+    fr = FrameRenderer(dim=DIM, table=table)
+
+    def ours(mode):
+        st = ViewState(b_xyz=(5, 95), b_view=(5, 95), render_mode=mode)
+        return fr.render(p, c2w, K, WIDTH, HEIGHT, st)
+
+    def med(fn):
+        fn()
+        fn()
+        ts = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            ts.append((time.perf_counter() - t0) * 1e3)
+        return sorted(ts)[len(ts) // 2]
+
+    with torch.no_grad():
+        res = {"rgb_ms": med(lambda: ours("RGB")), "depth_ms": med(lambda: ours("Depth")),
+               "steps_rgb_ms": med(lambda: steps("RGB")),
+               "steps_depth_ms": med(lambda: steps("Depth"))}
+    res["rgb_speedup"] = res["steps_rgb_ms"] / res["rgb_ms"]
+    res["depth_speedup"] = res["steps_depth_ms"] / res["depth_ms"]
+    res["what"] = ("viewer frame, 1M primitives, 1920x1080, Beta quantile ranges 5-95 %%, to a "
+                   "host float32 array: ubs.viewer vs the reference's view() steps on the "
+                   "drop-in operators; median wall clock of %d frames" % reps)
+    return res
+
+
 def time_steps(fn, K, dev, flush, after=None):
     """Per-step CUDA-event time (ms), L2 flushed before every step (untimed);
     `after` runs after each step, outside the timed events."""
@@ -1094,6 +1173,12 @@ def main():
         scene_file = bench_scene_file(p, dev)
     except Exception as e:  # noqa: BLE001
         scene_file = {"error": repr(e)[:300]}
+    viewer = None
+    try:
+        viewer = bench_viewer(p, cam, dev)
+    except Exception as e:  # noqa: BLE001
+        viewer = {"error": repr(e)[:300]}
+    torch.cuda.empty_cache()
 
     # the drop-in operator sequence (gsplat.rendering.rasterization call path)
     d_step = lambda: gpu_step(p, cam, ri, rj, bg, target)  # noqa: E731
@@ -1214,6 +1299,7 @@ def main():
             "loss": loss_res,
             "densify": densify,
             "scene_file": scene_file,
+            "viewer": viewer,
             "eager": {"value": 1000.0 / eager_ms, "unit": "it/s", "ms_per_step": eager_ms,
                       "what": "the same fused step launched kernel by kernel (no graph)"},
             "dropin": {"value": 1000.0 / d_ms, "unit": "it/s", "ms_per_step": d_ms,

@@ -358,6 +358,32 @@ int ubs_ply_unpack(const ubs_ply_layout *layout, const float *records, int64_t n
 int ubs_ply_pack(const ubs_ply_layout *layout, float *records, int64_t n_vertices,
                  void *stream);
 
+/* ---------------------------------------------------------------- viewer ---
+ * Per-frame work of the reference's viewer render (BetaModel.view,
+ * scene/beta_model.py:725-831) besides the render itself.
+ * ubs_quantile_mask: mask[i] = 1 where every value array a lies within
+ * [quantile(lo_a), quantile(hi_a)] of its n values -- quantiles[] = {lo, hi}
+ * per array, in [0, 1] -- with torch.quantile's linear interpolation (rank
+ * q (n - 1) in float32; a NaN value makes that array's bounds NaN and the
+ * mask 0).  arrays[a] (device) has element stride strides[a]; the viewer's
+ * arrays are raw_beta[:, 0], raw_beta[:, 1:4].mean(-1) and, 7-D,
+ * raw_beta[:, 4] (quantile_mask, scene/beta_model.py:729-757).  The order
+ * statistics are exact (radix select on the device).
+ * ubs_quantile_mask_bounds copies the 2 n_arrays bounds of the last mask
+ * computed in `workspace` to device memory.
+ * ubs_depth_colormap (utils/general_utils.py:172-218): out[i] = table[idx]
+ * (table: device float [256][3]) with idx = trunc(255 clip((x - min) /
+ * (max - min + 1e-10), 0, 1)) over the image's own min and max, NaN -> 0;
+ * workspace: 16 bytes of device memory. */
+size_t ubs_quantile_mask_workspace_bytes(void);
+int ubs_quantile_mask(int64_t n, int32_t n_arrays, const float *const *arrays,
+                      const int64_t *strides, const double *quantiles, uint8_t *mask,
+                      void *workspace, size_t workspace_bytes, void *stream);
+int ubs_quantile_mask_bounds(const void *workspace, int32_t n_arrays, float *bounds_out,
+                             void *stream);
+int ubs_depth_colormap(const float *image, int64_t n_pixels, const float *table, float *out,
+                       void *workspace, void *stream);
+
 /* Forward blend without a workspace (no counterpart in the reference).
  * Same arguments, results and errors as ubs_raster_fwd minus the workspace,
  * for callers that cannot allocate device memory where they render (a host
@@ -413,6 +439,29 @@ int ubs_scene_forward(int32_t dim, int64_t N, const float *xyz, const float *mea
                       const float *backgrounds, float *render_colors, float *render_alphas,
                       int32_t *last_ids, int64_t capacity, void *workspace,
                       size_t workspace_bytes, void *stream);
+/* Byte offsets, inside a forward's workspace, of the per-(view, primitive)
+ * radii (int32 [C, N]; 0: not rendered) and depths (float [C, N]) it leaves
+ * there -- the reference's meta["radii"] / meta["depths"]. */
+int ubs_scene_workspace_offsets(int32_t C, int64_t N, int32_t n_buckets, int64_t capacity,
+                                int64_t *radius_offset, int64_t *depth_offset);
+/* ubs_scene_forward with two viewer options (scene/beta_model.py:725-831):
+ * prim_mask (device uint8 [N], or NULL) leaves out primitives whose entry is
+ * 0 -- the same image as rendering the masked subset, as the reference's
+ * means[mask] ... does; color_mode 1 renders each primitive's depth in
+ * channel 0 (channels 1, 2 zero; one view; forward only), the reference's
+ * "Depth" mode when the backgrounds are zero. */
+int ubs_scene_forward_masked(int32_t dim, int64_t N, const float *xyz, const float *mean,
+                             const float *scale, const float *l_triangle, const float *opacity,
+                             const float *beta, const float *rgb, int32_t C,
+                             const float *viewmats, const float *intrinsics,
+                             const float *centers, const float *timestamps,
+                             const int32_t *view_dims, const int32_t *tile_base,
+                             const int64_t *pix_base, int32_t n_buckets, int32_t tile_size,
+                             float eps2d, float near_plane, float far_plane, float radius_clip,
+                             const float *backgrounds, float *render_colors,
+                             float *render_alphas, int32_t *last_ids, int64_t capacity,
+                             void *workspace, size_t workspace_bytes, const uint8_t *prim_mask,
+                             int32_t color_mode, void *stream);
 int ubs_scene_backward(int32_t dim, int64_t N, const float *xyz, const float *mean,
                        const float *scale, const float *l_triangle, const float *opacity,
                        const float *beta, const float *rgb, int32_t C, const float *viewmats,

@@ -58,8 +58,9 @@ def test_round_trip_one_million(tmp_path):
         q = ply.load_ply(path, DEV)
     finally:
         ply.CHUNK_BYTES = old_chunk
-    assert os.path.getsize(path) == 1_000_000 * 35 * 4 + len(
-        orc.ply_bytes({k: v[:0].cpu().numpy() for k, v in p.items()}))
+    n, names, off = ply.read_header(path)
+    assert n == 1_000_000 and len(names) == 35
+    assert os.path.getsize(path) == off + 1_000_000 * 35 * 4
     for k in ply.NAMES:
         assert torch.equal(q[k], p[k].reshape(p[k].shape[0], -1)), k
 

@@ -211,11 +211,11 @@ int ubs_ply_write(const char *path, int64_t n_vertices, int32_t n_props, const c
 
 static int ply_launch(const ubs_ply_layout *layout, float *records, int64_t n, void *stream,
                       bool pack) {
+    UBS_REQUIRE(n >= 0 && (records || n == 0), "ply: bad records");
+    if (n == 0) return UBS_OK; // nothing to move (empty tensors have no storage)
     PlyMap m;
     const int rc = load_map(layout, m);
     if (rc != UBS_OK) return rc;
-    UBS_REQUIRE(n >= 0 && (records || n == 0), "ply: bad records");
-    if (n == 0) return UBS_OK;
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

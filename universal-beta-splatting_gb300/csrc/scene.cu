@@ -65,6 +65,8 @@ struct SceneArgs {
     const float *viewmats, *intr, *centers, *times;
     const int32_t *dims, *tile_base;
     float tile_size, eps2d, near_p, far_p, radius_clip;
+    const uint8_t *prim_mask; // optional: primitives with 0 are not rendered
+    int color_mode;           // 0: rgb; 1: depth in channel 0 (one view, forward only)
     // outputs / workspace
     Rec *recs;
     float4 *cols_n; // colour row per primitive (written by the view-0 entries)
@@ -195,7 +197,8 @@ template <int D> __global__ void scene_prim_fwd_kernel(SceneArgs a) {
     world_to_cam(cam, f.om, pc);
     Proj2D p;
     p.radius = 0;
-    if (!(pc[2] < a.near_p || pc[2] > a.far_p)) {
+    const bool shown = !a.prim_mask || a.prim_mask[n] != 0;
+    if (shown && !(pc[2] < a.near_p || pc[2] > a.far_p)) {
         const M3 Sw = upper_sym(f.oV);
         const M3 Sc = mm(mm(cam.R, Sw), tr(cam.R));
         p = project_2d(pc, Sc, cam, W, H, a.eps2d, a.radius_clip);
@@ -216,8 +219,12 @@ template <int D> __global__ void scene_prim_fwd_kernel(SceneArgs a) {
     float4 *dst = reinterpret_cast<float4 *>(a.recs + idx);
     dst[0] = make_float4(r.x, r.y, r.opac, r.beta);
     dst[1] = make_float4(r.cxx, r.cxy, r.cyy, __int_as_float(r.gid));
-    if (v == 0) // one colour row per primitive for the sorted-record gather
-        a.cols_n[n] = make_float4(a.rgb[n * 3], a.rgb[n * 3 + 1], a.rgb[n * 3 + 2], 0.f);
+    if (v == 0) { // one colour row per primitive for the sorted-record gather
+        if (a.color_mode == 1)
+            a.cols_n[n] = make_float4(p.radius > 0 ? p.depth : 0.f, 0.f, 0.f, 0.f);
+        else
+            a.cols_n[n] = make_float4(a.rgb[n * 3], a.rgb[n * 3 + 1], a.rgb[n * 3 + 2], 0.f);
+    }
     a.radius[idx] = p.radius;
     a.depth[idx] = p.radius > 0 ? p.depth : 0.f;
     if (p.radius <= 0) return;
@@ -528,6 +535,15 @@ size_t ubs_scene_workspace_bytes(int32_t C, int64_t N, int32_t n_buckets, int64_
     return scene_ws(nullptr, C, N, n_buckets, capacity < 1 ? 1 : capacity).bytes;
 }
 
+int ubs_scene_workspace_offsets(int32_t C, int64_t N, int32_t n_buckets, int64_t capacity,
+                                int64_t *radius_offset, int64_t *depth_offset) {
+    UBS_REQUIRE(radius_offset && depth_offset, "scene_workspace_offsets: null output");
+    const SceneWs w = scene_ws(nullptr, C, N, n_buckets, capacity < 1 ? 1 : capacity);
+    *radius_offset = (int64_t)reinterpret_cast<uintptr_t>(w.radius);
+    *depth_offset = (int64_t)reinterpret_cast<uintptr_t>(w.depth);
+    return UBS_OK;
+}
+
 int ubs_scene_forward(int32_t dim, int64_t N, const float *xyz, const float *mean,
                       const float *scale, const float *l_triangle, const float *opacity,
                       const float *beta, const float *rgb, int32_t C, const float *viewmats,
@@ -538,11 +554,35 @@ int ubs_scene_forward(int32_t dim, int64_t N, const float *xyz, const float *mea
                       const float *backgrounds, float *render_colors, float *render_alphas,
                       int32_t *last_ids, int64_t capacity, void *workspace,
                       size_t workspace_bytes, void *stream) {
+    return ubs_scene_forward_masked(dim, N, xyz, mean, scale, l_triangle, opacity, beta, rgb, C,
+                                    viewmats, intrinsics, centers, timestamps, view_dims,
+                                    tile_base, pix_base, n_buckets, tile_size, eps2d, near_plane,
+                                    far_plane, radius_clip, backgrounds, render_colors,
+                                    render_alphas, last_ids, capacity, workspace,
+                                    workspace_bytes, nullptr, 0, stream);
+}
+
+int ubs_scene_forward_masked(int32_t dim, int64_t N, const float *xyz, const float *mean,
+                             const float *scale, const float *l_triangle, const float *opacity,
+                             const float *beta, const float *rgb, int32_t C,
+                             const float *viewmats, const float *intrinsics,
+                             const float *centers, const float *timestamps,
+                             const int32_t *view_dims, const int32_t *tile_base,
+                             const int64_t *pix_base, int32_t n_buckets, int32_t tile_size,
+                             float eps2d, float near_plane, float far_plane, float radius_clip,
+                             const float *backgrounds, float *render_colors,
+                             float *render_alphas, int32_t *last_ids, int64_t capacity,
+                             void *workspace, size_t workspace_bytes, const uint8_t *prim_mask,
+                             int32_t color_mode, void *stream) {
     SceneArgs a{};
     if (int e = scene_common(a, dim, N, xyz, mean, scale, l_triangle, opacity, beta, rgb, C,
                              viewmats, intrinsics, centers, timestamps, view_dims, tile_base,
                              tile_size, eps2d, near_plane, far_plane, radius_clip))
         return e;
+    UBS_REQUIRE(color_mode == 0 || (color_mode == 1 && C == 1),
+                "scene_forward: colour mode %d (0 rgb; 1 depth, one view)", color_mode);
+    a.prim_mask = prim_mask;
+    a.color_mode = color_mode;
     UBS_REQUIRE(n_buckets >= 1 && capacity >= 1 && pix_base && render_colors && render_alphas &&
                     last_ids,
                 "scene_forward: bad buckets / capacity / outputs");

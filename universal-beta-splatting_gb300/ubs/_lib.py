@@ -61,6 +61,10 @@ SIGNATURES = {
     "ubs_scene_workspace_bytes": ([_I32, _I64, _I32, _I64], _SZ),
     "ubs_scene_forward": ([_I32, _I64] + [_P] * 7 + [_I32] + [_P] * 7 + [_I32, _I32, _F, _F, _F, _F]
                           + [_P] * 4 + [_I64, _P, _SZ, _P], _INT),
+    "ubs_scene_workspace_offsets": ([_I32, _I64, _I32, _I64, _I64P, _I64P], _INT),
+    "ubs_scene_forward_masked": ([_I32, _I64] + [_P] * 7 + [_I32] + [_P] * 7
+                                 + [_I32, _I32, _F, _F, _F, _F] + [_P] * 4
+                                 + [_I64, _P, _SZ, _P, _I32, _P], _INT),
     "ubs_scene_backward": ([_I32, _I64] + [_P] * 7 + [_I32] + [_P] * 7 + [_I32, _I32, _F, _F, _F, _F]
                            + [_P] * 5 + [_P] * 7 + [_I32, _I64, _P, _SZ, _P], _INT),
     "ubs_scene_stats": ([_P, _I64P, _U32P, _P], _INT),
@@ -72,6 +76,10 @@ SIGNATURES = {
     "ubs_adam_table_bytes": ([_I32], _SZ),
     "ubs_adam_table_entry": ([_P, _I32, _P, _P, _P, _P, _I64, _I32], _INT),
     "ubs_adam_step": ([_I32, _P, _P, _I64, _F, _F, _F, _F, _P], _INT),
+    "ubs_quantile_mask_workspace_bytes": ([], _SZ),
+    "ubs_quantile_mask": ([_I64, _I32, _P, _P, _P, _P, _P, _SZ, _P], _INT),
+    "ubs_quantile_mask_bounds": ([_P, _I32, _P, _P], _INT),
+    "ubs_depth_colormap": ([_P, _I64, _P, _P, _P, _P], _INT),
     "ubs_ply_read_header": ([ctypes.c_char_p, _I64P, ctypes.POINTER(ctypes.c_int32), _P, _I32,
                              _I64P], _INT),
     "ubs_ply_read_body": ([ctypes.c_char_p, _I64, _P, _I64], _INT),

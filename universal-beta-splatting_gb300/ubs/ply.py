@@ -15,6 +15,7 @@ the inverse (one gather kernel, one copy to the host, one write).
     save_model_ply(model, path)      BetaModel.save_ply drop-in
 """
 import ctypes
+import math
 import os
 
 import torch
@@ -139,7 +140,10 @@ def load_ply(path, device="cuda"):
 @torch.no_grad()
 def save_ply(path, params):
     """Write raw parameter tensors (the reference's names) as its PLY file."""
-    t = {k: params[k].detach().reshape(params[k].shape[0], -1).contiguous() for k in NAMES}
+    t = {}
+    for k in NAMES:
+        v = params[k].detach()
+        t[k] = v.reshape(v.shape[0], int(math.prod(v.shape[1:]))).contiguous()
     n = t["xyz"].shape[0]
     dev = t["xyz"].device
     if not t["xyz"].is_cuda:

@@ -49,8 +49,11 @@ class Views:
             f[v, 0:16] = vm
             K = c.K.detach().float().cpu()
             f[v, 16:20] = torch.stack([K[0, 0], K[1, 1], K[0, 2], K[1, 2]])
-            R, t = vm.view(4, 4)[:3, :3], vm.view(4, 4)[:3, 3]
-            f[v, 20:23] = -R.t() @ t
+            if getattr(c, "position", None) is not None:
+                f[v, 20:23] = c.position.detach().reshape(3).float().cpu()
+            else:
+                R, t = vm.view(4, 4)[:3, :3], vm.view(4, 4)[:3, 3]
+                f[v, 20:23] = -R.t() @ t
             f[v, 23] = float(c.timestamp)
             tw = (c.width + tile_size - 1) // tile_size
             th = (c.height + tile_size - 1) // tile_size
@@ -155,6 +158,16 @@ class Renderer:
     def workspace_bytes(self, C, N, n_buckets, capacity):
         return L.query("ubs_scene_workspace_bytes", C, N, n_buckets, capacity)
 
+    def radii(self, views: Views, N: int):
+        """The last forward's per-(view, primitive) radii, int32 [C, N] (a view
+        into its workspace; 0 where a primitive was not rendered)."""
+        import ctypes
+        r, d = ctypes.c_int64(), ctypes.c_int64()
+        L.call("ubs_scene_workspace_offsets", views.C, N, views.n_buckets, self.last_cap,
+               ctypes.byref(r), ctypes.byref(d))
+        n = views.C * N
+        return self.last_ws[r.value:r.value + 4 * n].view(torch.int32).view(views.C, N)
+
     def _args(self, p, views, bg):
         return [self.dim, p["xyz"].shape[0]] + [L.ptr(p[k]) for k in PARAM_ORDER] + [
             views.C, L.ptr(views.viewmats), L.ptr(views.intr), L.ptr(views.centers),
@@ -162,14 +175,17 @@ class Renderer:
             views.n_buckets, self.tile_size, float(self.eps2d), float(self.near), float(self.far),
             float(self.radius_clip), L.ptr(bg)]
 
-    def forward_raw(self, p: Dict[str, torch.Tensor], views: Views, bg, check=True):
+    def forward_raw(self, p: Dict[str, torch.Tensor], views: Views, bg, check=True,
+                    prim_mask=None, color_mode=0):
         """Run the forward kernels; returns (colors, alphas, last_ids, workspace, capacity).
 
         check=True reads the intersection count back (synchronising) and
         re-runs an overflowing frame; check=False reads it back
         asynchronously and reports an overflow at the next call; check="none"
         issues nothing but the kernels (safe inside CUDA graph capture) and
-        leaves the verification to `stats()` after the frame(s)."""
+        leaves the verification to `stats()` after the frame(s).
+        prim_mask (uint8 [N]) leaves out primitives whose entry is 0;
+        color_mode=1 renders depth into channel 0 (one view, no backward)."""
         if check == "none":
             if self.capacity is None:
                 raise RuntimeError("check='none' needs a capacity (render once with check=True)")
@@ -185,8 +201,13 @@ class Renderer:
             alphas = torch.empty(views.n_pixels, device=dev)
             last = torch.empty(views.n_pixels, dtype=torch.int32, device=dev)
             st = L.stream(dev)
-            L.call("ubs_scene_forward", *self._args(p, views, bg), L.ptr(colors), L.ptr(alphas),
-                   L.ptr(last), cap, L.ptr(ws), ws.numel(), st)
+            if prim_mask is None and color_mode == 0:
+                L.call("ubs_scene_forward", *self._args(p, views, bg), L.ptr(colors),
+                       L.ptr(alphas), L.ptr(last), cap, L.ptr(ws), ws.numel(), st)
+            else:
+                L.call("ubs_scene_forward_masked", *self._args(p, views, bg), L.ptr(colors),
+                       L.ptr(alphas), L.ptr(last), cap, L.ptr(ws), ws.numel(),
+                       L.ptr(prim_mask, torch.uint8), int(color_mode), st)
             self.last_ws, self.last_cap = ws, cap
             if check == "none":
                 return colors, alphas, last, ws, cap

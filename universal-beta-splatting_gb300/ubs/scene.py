@@ -36,9 +36,12 @@ class Camera:
     width: int
     height: int
     timestamp: float = 0.0
+    position: Optional[torch.Tensor] = None  # camera centre; default -R^T t of the viewmat
 
     @property
     def center(self) -> torch.Tensor:
+        if self.position is not None:
+            return self.position
         R = self.viewmat[:3, :3]
         t = self.viewmat[:3, 3]
         return -R.t() @ t
