@@ -95,9 +95,15 @@ static int prof_sample_locked() {
         ProfSlot &p = g_prof_slots[i];
         if (!p.name) continue;
         float ms = 0.f;
-        if (cudaEventSynchronize(p.e1) != cudaSuccess ||
-            cudaEventElapsedTime(&ms, p.e0, p.e1) != cudaSuccess)
-            return check_launch("profile sample");
+        if (cudaEventSynchronize(p.e1) != cudaSuccess) return check_launch("profile sample");
+        const cudaError_t et = cudaEventElapsedTime(&ms, p.e0, p.e1);
+        if (et == cudaErrorInvalidResourceHandle) {
+            // a pair captured into a graph that has not been replayed yet:
+            // never recorded, nothing to add
+            cudaGetLastError();
+            continue;
+        }
+        if (et != cudaSuccess) return check_launch("profile sample");
         p.acc_ms += ms;
         p.n += 1;
     }
