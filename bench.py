@@ -39,9 +39,16 @@ import torch  # noqa: E402
 
 METRIC = "render FPS and train it/s at 1M prims 1080p; serving p50/p99 ms vs plain form"
 N_PRIMS, DIM, WIDTH, HEIGHT, FOCAL, TILE = 1_000_000, 6, 1920, 1080, 1500.0, 16
-# FP32 operations (FMA = 2) per contributing (pixel, primitive) pair in the
-# reference's per-pair arithmetic (rasterize_to_pixels_fwd.cu:140-171,
-# rasterize_to_pixels_bwd.cu:170-247); rejected pairs are not counted.
+# Blend work units for the roofline.  Primary (the hot-path scope table's
+# definition): a (pixel, record) pair a per-pixel loop evaluates -- forward:
+# every record of the pixel's tile up to the one that ends it, else the whole
+# range, ~20 FP32 operations + 1 pow counted as 2 MUFU operations; backward:
+# records up to the pixel's last contributor, ~45 FP32 + 3 MUFU-class
+# operations (rasterize_to_pixels_fwd.cu:140-171, rasterize_to_pixels_bwd.cu:
+# 170-247).  Secondary: contributing pairs only, with this kernel's own
+# operation counts (FMA = 2).
+FWD_OPS_PER_EVAL_PAIR = 22
+BWD_OPS_PER_EVAL_PAIR = 48
 FWD_FLOP_PER_PAIR = 28
 BWD_FLOP_PER_PAIR = 77
 # FP32 operations per (pixel, channel) of the SSIM training loss and its
@@ -619,7 +626,8 @@ def fp32_peak(dev):
 
 
 def count_pairs(p, cam, ri, rj, bg, dev):
-    """Contributing (pixel, primitive) pairs of one forward (device counter)."""
+    """(contributing pairs, intersections, visible primitives, evaluated
+    forward pairs, backward pairs) of one forward (device counters)."""
     import ctypes
     from gsplat.cuda import _wrapper as Wr
     from ubs import _lib as L
@@ -642,11 +650,11 @@ def count_pairs(p, cam, ri, rj, bg, dev):
         L.call("ubs_raster_fwd_packed", C, N, 3, T, L.ptr(colors), L.ptr(bg.view(1, 3)), None,
                WIDTH, HEIGHT, TILE, meta["tile_width"], meta["tile_height"], L.ptr(offs),
                L.ptr(oc), L.ptr(oa), L.ptr(li), 1, L.ptr(ws), ws.numel(), st)
-        status = ctypes.c_uint32(0)
-        pairs = ctypes.c_uint64(0)
-        L.call("ubs_raster_status", L.ptr(ws), ctypes.byref(status), ctypes.byref(pairs), st)
+        counts = (ctypes.c_uint64 * 3)()
+        L.call("ubs_raster_pair_counts", L.ptr(ws), ctypes.cast(counts, ctypes.c_void_p), st)
         del Wr
-        return int(pairs.value), int(T), int((meta["radii"] > 0).sum())
+        return (int(counts[0]), int(T), int((meta["radii"] > 0).sum()), int(counts[1]),
+                int(counts[2]))
 
 
 def read_profile_traffic(kernel):
@@ -1195,7 +1203,7 @@ def main():
             S.render_view(p, cam, bg, ri, rj, tile_size=TILE)
     d_fwd_ms = time_steps(d_fwd, K2, dev, flush)
 
-    pairs, n_isects, n_visible = count_pairs(p, cam, ri, rj, bg, dev)
+    pairs, n_isects, n_visible, eval_pairs, bwd_pairs = count_pairs(p, cam, ri, rj, bg, dev)
     peak_fp32 = fp32_peak(dev)
     peaks = {}
     try:
@@ -1205,14 +1213,23 @@ def main():
     dominant = max(kernel_ms, key=kernel_ms.get)
     n_dom, t_dom = kernels[dominant]
     dom_ms = t_dom / n_dom
-    flop_pp = BWD_FLOP_PER_PAIR if dominant == "raster_bwd" else FWD_FLOP_PER_PAIR
-    achieved = pairs * flop_pp / (dom_ms * 1e-3) / 1e12
+    is_bwd = dominant == "raster_bwd"
+    units = bwd_pairs if is_bwd else eval_pairs
+    ops = BWD_OPS_PER_EVAL_PAIR if is_bwd else FWD_OPS_PER_EVAL_PAIR
+    achieved = units * ops / (dom_ms * 1e-3) / 1e12
+    flop_pp = BWD_FLOP_PER_PAIR if is_bwd else FWD_FLOP_PER_PAIR
+    contrib_achieved = pairs * flop_pp / (dom_ms * 1e-3) / 1e12
     roofline = {
         "kernel": dominant, "bound": "fp32",
         "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s",
         "frac": achieved / peak_fp32 if peak_fp32 else None,
         "traffic": read_profile_traffic(dominant),
-        "algorithmic_work": "%d contributing pairs x %d FP32 ops per launch" % (pairs, flop_pp),
+        "algorithmic_work": "%d %s pairs x %d operations (FP32 + MUFU) per launch" % (
+            units, "backward (records up to each pixel's last contributor)" if is_bwd else
+            "evaluated", ops),
+        "contributing_pairs": {"pairs": pairs, "ops_per_pair": flop_pp,
+                               "achieved": contrib_achieved,
+                               "frac": contrib_achieved / peak_fp32 if peak_fp32 else None},
         "peak_source": "measured: FP32 FMA probe kernel timed in this run (MEASURED_PEAKS.json "
                        "has HBM %s GB/s and bf16 only)" % peaks.get("hbm_gbs", "n/a"),
         "launch_ms": dom_ms,
@@ -1309,6 +1326,7 @@ def main():
             "kernels_ms_per_step": {k: round(v, 4) for k, v in
                                     sorted(kernel_ms.items(), key=lambda x: -x[1])},
             "isects": n_isects, "visible": n_visible, "pairs": pairs,
+            "evaluated_pairs": eval_pairs, "backward_pairs": bwd_pairs,
             "wall_s_timed": wall,
             "configs": configs,
         }

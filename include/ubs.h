@@ -484,6 +484,12 @@ int ubs_scene_stats(const void *workspace, int64_t *n_isects, uint32_t *status, 
  * blend on `workspace` (pair_count may be NULL); synchronises the stream. */
 int ubs_raster_status(const void *workspace, uint32_t *status, uint64_t *pair_count,
                       void *stream);
+/* After a forward with count_pairs != 0: counts[0] contributing (pixel,
+ * record) pairs, counts[1] pairs a per-pixel blend loop evaluates (each
+ * pixel's records up to the one that ends it, else its tile's whole range),
+ * counts[2] pairs up to each pixel's last contributor (what the backward
+ * walks).  Synchronises the stream. */
+int ubs_raster_pair_counts(const void *workspace, uint64_t *counts, void *stream);
 
 #ifdef __cplusplus
 }

@@ -54,7 +54,10 @@ struct RasterArgs {
     const float *v_out_a;
     float *v_m2, *v_cn, *v_col, *v_op, *v_be;
     uint32_t *status;
-    unsigned long long *pair_count; // contributing (pixel, record) pairs, or nullptr
+    // counters of the COUNT forward, or nullptr: [0] contributing (pixel,
+    // record) pairs, [1] pairs a per-pixel loop evaluates up to termination,
+    // [2] pairs up to each pixel's last contributor
+    unsigned long long *pair_count;
     // multi-view grids (nullptr: C views of W x H with the same TW x TH grid)
     const int32_t *v_tile_base; // [C+1] first (view, tile) bucket of each view
     const int32_t *v_dims;      // [C, 4] width, height, tile columns, tile rows
@@ -273,7 +276,8 @@ template <int CD, bool COUNT>
 __device__ __forceinline__ void blend_pair(const GeoRec &q, const float (&col)[CD], float px,
                                            float2 npy, float2 &T, float2 (&acc)[CD],
                                            int32_t &cur0, int32_t &cur1, bool &d0, bool &d1,
-                                           int32_t idx, uint32_t &n_contrib) {
+                                           int32_t idx, uint32_t &n_contrib, int32_t &term0,
+                                           int32_t &term1) {
     const float dx = q.x - px;
     const float2 dy = __fadd2_rn(make_float2(q.y, q.y), npy);
     const float A = q.cxx * dx * dx;
@@ -305,7 +309,11 @@ __device__ __forceinline__ void blend_pair(const GeoRec &q, const float (&col)[C
     T.y = b1 ? n.y : T.y;
     cur0 = b0 ? idx : cur0;
     cur1 = b1 ? idx : cur1;
-    if (COUNT) n_contrib += (uint32_t)b0 + (uint32_t)b1;
+    if (COUNT) {
+        n_contrib += (uint32_t)b0 + (uint32_t)b1;
+        term0 = t0 ? idx : term0;
+        term1 = t1 ? idx : term1;
+    }
 }
 
 // --------------------------------------------------------------- forward
@@ -357,6 +365,7 @@ __global__ void __launch_bounds__(512) raster_fwd_kernel(RasterArgs a) {
     float2 T = make_float2(1.0f, 1.0f);
     int32_t cur0 = 0, cur1 = 0;
     uint32_t n_contrib = 0;
+    int32_t term0 = -1, term1 = -1; // COUNT: record at which a pixel terminated
     float2 acc[CD];
 #pragma unroll
     for (int k = 0; k < CD; ++k) acc[k] = make_float2(0.f, 0.f);
@@ -416,7 +425,7 @@ __global__ void __launch_bounds__(512) raster_fwd_kernel(RasterArgs a) {
                         float col[CD];
                         load_color<CD, PACK>(scol4, scol, buf * BR + t, col);
                         blend_pair<CD, COUNT>(q, col, px, npy, T, acc, cur0, cur1, d0, d1,
-                                              bs + t, n_contrib);
+                                              bs + t, n_contrib, term0, term1);
                         if (__all_sync(0xffffffffu, d0 && d1)) {
                             warp_done = true;
                             break;
@@ -436,6 +445,21 @@ __global__ void __launch_bounds__(512) raster_fwd_kernel(RasterArgs a) {
     if (COUNT) {
         const uint32_t w = __reduce_add_sync(0xffffffffu, n_contrib);
         if (lane == 0 && w) atomicAdd(a.pair_count, (unsigned long long)w);
+        // evaluated pairs of a per-pixel loop: up to the terminating record,
+        // else the whole range; backward pairs: up to the last contributor
+        uint32_t ev = 0, bw = 0;
+        if (in0) {
+            ev += (uint32_t)(term0 >= 0 ? term0 - rs + 1 : re - rs);
+            bw += (uint32_t)(cur0 >= rs && cur0 > 0 ? cur0 - rs + 1 : 0);
+        }
+        if (in1) {
+            ev += (uint32_t)(term1 >= 0 ? term1 - rs + 1 : re - rs);
+            bw += (uint32_t)(cur1 >= rs && cur1 > 0 ? cur1 - rs + 1 : 0);
+        }
+        const uint32_t we = __reduce_add_sync(0xffffffffu, ev);
+        const uint32_t wb = __reduce_add_sync(0xffffffffu, bw);
+        if (lane == 0 && we) atomicAdd(a.pair_count + 1, (unsigned long long)we);
+        if (lane == 0 && wb) atomicAdd(a.pair_count + 2, (unsigned long long)wb);
     }
     if (in0) {
         a.out_a[pix0] = 1.0f - T.x;
@@ -1065,6 +1089,19 @@ int ubs_raster_status(const void *workspace, uint32_t *status, uint64_t *pair_co
         return check_launch("raster_status");
     *status = (uint32_t)(hdr[0] & 0xffffffffu);
     if (pair_count) *pair_count = hdr[1];
+    return UBS_OK;
+}
+
+int ubs_raster_pair_counts(const void *workspace, uint64_t *counts, void *stream) {
+    UBS_REQUIRE(workspace && counts, "raster_pair_counts: null pointer");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    uint64_t hdr[4];
+    if (cudaMemcpyAsync(hdr, workspace, 32, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return check_launch("raster_pair_counts");
+    counts[0] = hdr[1];
+    counts[1] = hdr[2];
+    counts[2] = hdr[3];
     return UBS_OK;
 }
 

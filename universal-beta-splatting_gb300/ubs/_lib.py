@@ -61,6 +61,7 @@ SIGNATURES = {
     "ubs_scene_workspace_bytes": ([_I32, _I64, _I32, _I64], _SZ),
     "ubs_scene_forward": ([_I32, _I64] + [_P] * 7 + [_I32] + [_P] * 7 + [_I32, _I32, _F, _F, _F, _F]
                           + [_P] * 4 + [_I64, _P, _SZ, _P], _INT),
+    "ubs_raster_pair_counts": ([_P, _P, _P], _INT),
     "ubs_scene_workspace_offsets": ([_I32, _I64, _I32, _I64, _I64P, _I64P], _INT),
     "ubs_scene_forward_masked": ([_I32, _I64] + [_P] * 7 + [_I32] + [_P] * 7
                                  + [_I32, _I32, _F, _F, _F, _F] + [_P] * 4
