@@ -1105,9 +1105,43 @@ def main():
 
     for _ in range(2):
         e2e_step()
-    e2e_ms = time_steps(e2e_step, args.steps, dev, flush)
+    e2e_serial_ms = time_steps(e2e_step, args.steps, dev, flush)
     gs.check()
+    _, e2e_serial = replica_throughput(e2e_serial_ms, world, dev)
+
+    # the same, double-buffered through ubs.render.HostFedStep: step k+1's
+    # host-to-device copies run on a copy stream during step k's compute; the
+    # timed region spans K consecutive steps (every copy and loss read inside
+    # it; each step's 165 MB of fresh inputs exceeds the 129 MB L2)
+    from ubs.render import HostFedStep
+
+    def make_inputs():
+        q = {k: torch.nn.Parameter(v.detach().clone()) for k, v in p.items()}
+        t = g_target.clone()
+        return q, [q[k] for k in p] + [t], lambda c, a: (c - t).abs().mean()
+
+    hf = HostFedStep(Renderer(dim=DIM, tile_size=TILE), fz.views, fz.bg, make_inputs)
+    feed_host = [host[k] for k in p] + [host_target]
+    for _ in range(4):
+        hf.step(feed_host)
+    hf.losses()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    hf.start()
+    for _ in range(args.steps):
+        hf.step(feed_host)
+        if len(hf.pending) >= hf.ring - 1:
+            hf.losses()
+    e1.record()
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    e2e_losses = hf.losses()
+    hf.check()
     _, e2e_val = replica_throughput(e2e_ms, world, dev)
+    del hf
     clocks.stop()
     # the same step without the graph (one launch per kernel from the host)
     fz.prime()
@@ -1306,7 +1340,13 @@ def main():
                                "replayed as one CUDA graph (ubs.render.GraphedStep)"},
             "render_fps": 1000.0 / fwd_ms,
             "e2e": {"value": e2e_val, "unit": "it/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": 4},
+                    "d2h_bytes_per_step": 4, "ms_per_step": e2e_ms,
+                    "how": "ubs.render.HostFedStep: parameters and target copied from pinned "
+                           "host memory every step on a copy stream, double-buffered against "
+                           "the previous step's graph replay; loss read back every step; "
+                           "CUDA events around K consecutive steps",
+                    "serial": {"value": e2e_serial, "ms_per_step": e2e_serial_ms,
+                               "how": "copies, then the replay, per step on one stream"}},
             "gpu_launches": int(launches),
             "launches_per_step": int(launches) // max(1, args.steps),
             "roofline": roofline,

@@ -359,3 +359,81 @@ class GraphedStep:
 
     def check(self):
         return self.r.stats()
+
+
+class HostFedStep:
+    """Steps whose inputs come from pinned host memory every step (a data
+    loader, another process, a parameter store), with the copies of step k+1
+    overlapping the compute of step k.
+
+    `make_inputs()` returns (params, feeds, loss_fn): the parameter tensors
+    of a GraphedStep, the device tensors that receive the host data each step
+    (any of the parameters and, e.g., a target image the loss reads), and
+    the loss over (colors, alphas).  It is called `depth` times (default 2):
+    each buffer set gets its own tensors and its own captured step.
+    `step(host)` copies host[i] (pinned, same shapes as feeds[i]) into the
+    next set's feeds on a copy stream once that set's previous step is done,
+    replays the set's graph on the current stream once the copies are done,
+    and copies the loss into a pinned slot; `losses()` waits for the device
+    and returns the values of the steps since the last call.  `start()` makes
+    the copy stream wait for the current stream's work issued so far (call it
+    where a timed region begins)."""
+
+    def __init__(self, renderer: Renderer, views: Views, backgrounds, make_inputs,
+                 depth: int = 2, headroom: float = 1.5, warmup: int = 3):
+        if depth < 1:
+            raise ValueError("depth must be >= 1")
+        self.sets = []
+        for _ in range(depth):
+            params, feeds, loss_fn = make_inputs()
+            gs = GraphedStep(renderer, params, views, backgrounds, loss_fn, headroom, warmup)
+            self.sets.append((gs, list(feeds)))
+        self.device = self.sets[0][1][0].device
+        self.copy_stream = torch.cuda.Stream(self.device)
+        self.copied = [torch.cuda.Event() for _ in range(depth)]
+        self.done = [None] * depth
+        self.ring = 256
+        self.loss_host = torch.empty(self.ring, pin_memory=True)
+        self.k = 0
+        self.pending = []
+        self.launches_per_step = self.sets[0][0].launches_per_replay
+
+    def start(self):
+        ev = torch.cuda.Event()
+        ev.record(torch.cuda.current_stream(self.device))
+        self.copy_stream.wait_event(ev)
+
+    def step(self, host: Sequence[torch.Tensor]):
+        s = self.k % len(self.sets)
+        gs, feeds = self.sets[s]
+        if len(host) != len(feeds):
+            raise ValueError("step() needs one host tensor per feed")
+        cs = self.copy_stream
+        cur = torch.cuda.current_stream(self.device)
+        if self.done[s] is not None:
+            cs.wait_event(self.done[s])  # the set's previous step has read its inputs
+        with torch.cuda.stream(cs), torch.no_grad():
+            for dst, src in zip(feeds, host):
+                dst.copy_(src, non_blocking=True)
+        self.copied[s].record(cs)
+        cur.wait_event(self.copied[s])
+        loss = gs.replay()
+        slot = self.k % self.ring
+        if len(self.pending) == self.ring:
+            raise RuntimeError("call losses() at least every %d steps" % self.ring)
+        self.loss_host[slot:slot + 1].copy_(loss.detach().view(1), non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(cur)
+        self.done[s] = ev
+        self.pending.append(slot)
+        self.k += 1
+        return slot
+
+    def losses(self) -> List[float]:
+        torch.cuda.current_stream(self.device).synchronize()
+        out = [float(self.loss_host[i]) for i in self.pending]
+        self.pending = []
+        return out
+
+    def check(self):
+        return [gs.check() for gs, _ in self.sets]
