@@ -261,9 +261,11 @@ int ubs_adam_step(int32_t n_tensors, const void *device_table, const float *devi
  * at img + n s[0] + c s[1] + y s[2] + x s[3] for its strides s (int64[4]);
  * gt and grad likewise.  grad == NULL computes the loss only.
  * out (device, float[3]) receives mean(map), mean|img - gt| and the loss.
- * The workspace (ubs_ssim_workspace_bytes) must be zero before its first use;
- * every call leaves it zero again, so it can be reused by calls ordered on one
- * stream (and by a captured launch). */
+ * Two launches with the gradient (map and derivatives; the gradient), one
+ * without.  The workspace (ubs_ssim_workspace_bytes: a header, per-CTA
+ * partials and three derivative planes of the batch) needs only its first 256
+ * bytes zero before its first use; every call leaves them zero again, so it
+ * can be reused by calls ordered on one stream (and by captured launches). */
 size_t ubs_ssim_workspace_bytes(int32_t n_images, int32_t channels, int32_t height,
                                 int32_t width);
 int ubs_ssim_loss(const float *img, const int64_t *img_strides, const float *gt,

@@ -1,5 +1,4 @@
-// ssim.cu -- the training loss (1 - l) L1 + l (1 - SSIM) and its gradient in
-// one pass.
+// ssim.cu -- the training loss (1 - l) L1 + l (1 - SSIM) and its gradient.
 //
 // SSIM as the reference defines it (utils/loss_utils.py:26-80, the function
 // the fused_ssim package used by train.py:117-121 evaluates): an 11 x 11
@@ -9,19 +8,22 @@
 // with sxx = E[x^2] - mx^2, sxy = E[xy] - mx my, and the loss reads the mean
 // of the map (optionally cropped by the window radius, fused_ssim's "valid").
 //
-// One CTA owns a 32 x 32 tile of one (image, channel).  The window is
-// separable, so the moments are a horizontal then a vertical 11-tap pass over
-// shared memory.  For the gradient the CTA also evaluates the map on the
-// 5-pixel ring around its tile (recomputing the moments there from a 10-pixel
-// input halo) and forms, per map point q,
-//   D0 = d map / d mx,  D1 = d map / d E[x^2],  D2 = d map / d E[xy]
-// (derivatives with the E[.] moments as the free variables); the gradient at
-// pixel p is then  sum_q w(q - p) (D0 + 2 x_p D1 + y_p D2), two more
-// separable passes.  Nothing but the inputs and the gradient touches HBM.
-//
+// Two kernels, each over 32 x 32 tiles of one (image, channel); quantities
+// that are filtered with the same window travel in pairs through Blackwell's
+// packed FP32x2 FMA ((x, y), (x^2, y^2), (D1, D2)):
+//  * ssim_map_kernel: the five windowed moments of the tile (separable: a
+//    horizontal then a vertical 11-tap pass over shared memory, the products
+//    formed in registers), the map, the loss partials and -- for the
+//    gradient -- the map's derivatives with the E[.] moments as the free
+//    variables, D0 = d map / d mx, D1 = d map / d E[x^2],
+//    D2 = d map / d E[xy], stored as a D0 plane and a (D1, D2) plane (12 B
+//    per pixel-channel, mostly L2-resident between the two launches);
+//  * ssim_grad_kernel: d loss / d x_p = gb sum_q w(q - p) (D0 + 2 x_p D1 +
+//    y_p D2) + ga sign(x_p - y_p): the window over the three planes and the
+//    combination with the image and target.
 // Loss sums: one partial per CTA, reduced in a fixed order by the last CTA to
 // finish (a ticket counter that the last CTA resets), so the result is
-// deterministic and the launch can be replayed from a CUDA graph.
+// deterministic and the launches can be replayed from a CUDA graph.
 #include <cmath>
 
 #include "ubs_common.cuh"
@@ -29,10 +31,14 @@
 namespace ubs {
 namespace {
 
-constexpr int SS_T = 32;       // output tile edge
-constexpr int SS_R = 5;        // window radius (11 taps)
+constexpr int SS_T = 32;                // output tile edge
+constexpr int SS_R = 5;                 // window radius (11 taps)
 constexpr int SS_W = 2 * SS_R + 1;
-constexpr int SS_THREADS = 384;
+constexpr int SS_IN = SS_T + 2 * SS_R;  // 42: tile plus halo
+constexpr int SS_IP = SS_IN + 1;        // padded pitch of the halo planes
+constexpr int SS_HP = SS_T + 1;         // padded pitch of the horizontal results
+constexpr int SS_THREADS = 256;
+constexpr int SS_LOADS = (SS_IN * SS_IN + SS_THREADS - 1) / SS_THREADS; // halo loads per thread
 
 struct SsimArgs {
     const float *img;
@@ -47,27 +53,11 @@ struct SsimArgs {
     double inv_px, inv_map;      // 1 / pixels, 1 / counted map points
     double wl1, wssim, wconst;   // loss = wl1 mean|x-y| + wssim mean(map) + wconst
     float g[SS_W];               // normalised 1-D window
+    float *dmap0;                // [n c][h][w] D0 plane (gradient only)
+    float2 *dmap12;              // [n c][h][w] (D1, D2) plane
     float *partials;             // [n_ctas][2]
     unsigned *counter;
     float *out;                  // [3]: mean(map), mean|x-y|, loss
-};
-
-// Region sizes: the loss-only variant needs moments on the tile itself; the
-// gradient variant on the tile plus a ring of SS_R.
-template <bool GRAD> struct Geom {
-    static constexpr int MO = SS_T + (GRAD ? 2 * SS_R : 0); // moment / map points per edge
-    static constexpr int IN = MO + 2 * SS_R;                // input pixels per edge
-    static constexpr int IP = IN + 1;                       // padded pitch of input planes
-    static constexpr int MP = MO + 1;                       // padded pitch of moment planes
-    static constexpr int OFF = (IN - SS_T) / 2;             // tile origin inside the input region
-    static constexpr int SEG = GRAD ? 6 : 8;                // outputs per item, moment passes
-    static constexpr int NSEG = MO / SEG;
-    static_assert(MO % SEG == 0, "segments must tile the moment region");
-    // input planes x, y, x^2, y^2, xy; horizontal moments (5 planes IN x MO)
-    static constexpr int IN_PLANE = IN * IP;
-    static constexpr int HM_PLANE = IN * MP;
-    static constexpr size_t FLOATS = 5 * (size_t)IN_PLANE + 5 * (size_t)HM_PLANE;
-    static constexpr size_t BYTES = FLOATS * sizeof(float) + 64;
 };
 
 __device__ __forceinline__ float block_sum(float v, float *red) {
@@ -82,193 +72,48 @@ __device__ __forceinline__ float block_sum(float v, float *red) {
     return s; // valid in thread 0
 }
 
-template <bool GRAD>
-__global__ void __launch_bounds__(SS_THREADS, 2) ssim_kernel(const SsimArgs a) {
-    using G = Geom<GRAD>;
-    extern __shared__ float4 smem4[];
-    float *sm = reinterpret_cast<float *>(smem4);
-    float *in = sm;                         // 5 input planes
-    float *hm = sm + 5 * G::IN_PLANE;       // 5 horizontal-moment planes
+// 4 outputs of an 11-tap window over 14 consecutive values: scalar, and two
+// streams at once with the packed FP32x2 FMA (same rounding per component)
+__device__ __forceinline__ void taps4(const float (&g)[SS_W], const float (&v)[14],
+                                      float (&acc)[4]) {
+#pragma unroll
+    for (int o = 0; o < 4; ++o) acc[o] = 0.f;
+#pragma unroll
+    for (int t = 0; t < SS_W; ++t)
+#pragma unroll
+        for (int o = 0; o < 4; ++o) acc[o] = fmaf(g[t], v[o + t], acc[o]);
+}
+__device__ __forceinline__ void taps4x2(const float (&g)[SS_W], const float2 (&v)[14],
+                                        float2 (&acc)[4]) {
+#pragma unroll
+    for (int o = 0; o < 4; ++o) acc[o] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int t = 0; t < SS_W; ++t) {
+        const float2 g2 = make_float2(g[t], g[t]);
+#pragma unroll
+        for (int o = 0; o < 4; ++o) acc[o] = __ffma2_rn(g2, v[o + t], acc[o]);
+    }
+}
+
+// Asynchronous global -> shared copies of 4 or 8 bytes (no register staging,
+// so every halo load of a thread is in flight at once); src_bytes 0 writes
+// zeros, which is the window's zero padding outside the image.
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *dst, const void *src, bool in) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(d), "l"(src),
+                 "n"(BYTES), "r"(in ? BYTES : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+// the CTA's partials -> the last CTA reduces all of them in a fixed order
+__device__ void finish_loss(const SsimArgs &a, float ssim_sum, float l1_sum) {
     __shared__ float red[SS_THREADS / 32];
     __shared__ bool last;
-
-    const int img = blockIdx.z / a.c, ch = blockIdx.z % a.c;
-    const int y0 = blockIdx.y * SS_T, x0 = blockIdx.x * SS_T;
-    const float *X = a.img + img * a.is[0] + ch * a.is[1];
-    const float *Y = a.gt + img * a.gs[0] + ch * a.gs[1];
-
-    // ---- inputs (zero outside the image) and their products
-    for (int i = threadIdx.x; i < G::IN * G::IN; i += SS_THREADS) {
-        const int r = i / G::IN, cc = i % G::IN;
-        const int gy = y0 - G::OFF + r, gx = x0 - G::OFF + cc;
-        float xv = 0.f, yv = 0.f;
-        if (gy >= 0 && gy < a.h && gx >= 0 && gx < a.w) {
-            xv = __ldg(X + gy * a.is[2] + gx * a.is[3]);
-            yv = __ldg(Y + gy * a.gs[2] + gx * a.gs[3]);
-        }
-        const int o = r * G::IP + cc;
-        in[o] = xv;
-        in[G::IN_PLANE + o] = yv;
-        in[2 * G::IN_PLANE + o] = xv * xv;
-        in[3 * G::IN_PLANE + o] = yv * yv;
-        in[4 * G::IN_PLANE + o] = xv * yv;
-    }
-    __syncthreads();
-
-    // ---- horizontal pass: item = (row, segment); consecutive threads take
-    // consecutive rows (odd pitch: conflict-free)
-    for (int it = threadIdx.x; it < G::IN * G::NSEG; it += SS_THREADS) {
-        const int r = it % G::IN, c0 = (it / G::IN) * G::SEG;
-#pragma unroll 1
-        for (int k = 0; k < 5; ++k) {
-            const float *src = in + k * G::IN_PLANE + r * G::IP + c0;
-            float v[G::SEG + 2 * SS_R];
-#pragma unroll
-            for (int j = 0; j < G::SEG + 2 * SS_R; ++j) v[j] = src[j];
-            float acc[G::SEG];
-#pragma unroll
-            for (int o = 0; o < G::SEG; ++o) acc[o] = 0.f;
-#pragma unroll
-            for (int t = 0; t < SS_W; ++t) {
-                const float wt = a.g[t];
-#pragma unroll
-                for (int o = 0; o < G::SEG; ++o) acc[o] = fmaf(wt, v[o + t], acc[o]);
-            }
-            float *dst = hm + k * G::HM_PLANE + r * G::MP + c0;
-#pragma unroll
-            for (int o = 0; o < G::SEG; ++o) dst[o] = acc[o];
-        }
-    }
-    __syncthreads();
-
-    // ---- vertical pass, the map and (GRAD) its derivatives.  The product
-    // planes are free from here on: D0..D2 (MO x MP each) go there; x and y
-    // stay for the gradient.
-    float *dmap = in + 2 * G::IN_PLANE;
-    float ssim_sum = 0.f;
-    for (int it = threadIdx.x; it < G::MO * G::NSEG; it += SS_THREADS) {
-        const int m = it % G::MO, r0 = (it / G::MO) * G::SEG;
-        float mom[5][G::SEG];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            const float *src = hm + k * G::HM_PLANE + r0 * G::MP + m;
-            float v[G::SEG + 2 * SS_R];
-#pragma unroll
-            for (int j = 0; j < G::SEG + 2 * SS_R; ++j) v[j] = src[j * G::MP];
-#pragma unroll
-            for (int o = 0; o < G::SEG; ++o) mom[k][o] = 0.f;
-#pragma unroll
-            for (int t = 0; t < SS_W; ++t) {
-                const float wt = a.g[t];
-#pragma unroll
-                for (int o = 0; o < G::SEG; ++o) mom[k][o] = fmaf(wt, v[o + t], mom[k][o]);
-            }
-        }
-#pragma unroll
-        for (int o = 0; o < G::SEG; ++o) {
-            const int r = r0 + o;
-            const int gy = y0 - (G::MO - SS_T) / 2 + r, gx = x0 - (G::MO - SS_T) / 2 + m;
-            bool counted = gy >= 0 && gy < a.h && gx >= 0 && gx < a.w;
-            if (a.valid)
-                counted = counted && gy >= SS_R && gy < a.h - SS_R && gx >= SS_R && gx < a.w - SS_R;
-            const float mx = mom[0][o], my = mom[1][o];
-            const float mxx = mx * mx, myy = my * my, mxy = mx * my;
-            const float vx = mom[2][o] - mxx, vy = mom[3][o] - myy, cxy = mom[4][o] - mxy;
-            const float A1 = 2.f * mxy + a.c1, A2 = 2.f * cxy + a.c2;
-            const float B1 = mxx + myy + a.c1, B2 = vx + vy + a.c2;
-            const float s = (A1 * A2) / (B1 * B2);
-            const bool own = r >= (G::MO - SS_T) / 2 && r < (G::MO + SS_T) / 2 &&
-                             m >= (G::MO - SS_T) / 2 && m < (G::MO + SS_T) / 2;
-            if (counted && own) ssim_sum += s;
-            if (GRAD) {
-                float d0 = 0.f, d1 = 0.f, d2 = 0.f;
-                if (counted) {
-                    const float iB1 = 1.f / B1, iB2 = 1.f / B2, iBB = iB1 * iB2;
-                    d0 = 2.f * my * (A2 - A1) * iBB - 2.f * mx * s * (iB1 - iB2);
-                    d1 = -s * iB2;
-                    d2 = 2.f * A1 * iBB;
-                }
-                dmap[r * G::MP + m] = d0;
-                dmap[G::HM_PLANE + r * G::MP + m] = d1;
-                dmap[2 * G::HM_PLANE + r * G::MP + m] = d2;
-            }
-        }
-    }
-
-    float l1_sum = 0.f;
-    if (GRAD) {
-        __syncthreads();
-        // ---- horizontal pass over D0..D2 (MO rows -> SS_T columns), 16
-        // outputs per item; results into the moment planes (free now)
-        float *dh = hm;
-        constexpr int DSEG = 16, DNS = SS_T / DSEG;
-        for (int it = threadIdx.x; it < 3 * G::MO * DNS; it += SS_THREADS) {
-            const int r = it % G::MO, rest = it / G::MO;
-            const int c0 = (rest % DNS) * DSEG, k = rest / DNS;
-            const float *src = dmap + k * G::HM_PLANE + r * G::MP + c0;
-            float v[DSEG + 2 * SS_R];
-#pragma unroll
-            for (int j = 0; j < DSEG + 2 * SS_R; ++j) v[j] = src[j];
-            float acc[DSEG];
-#pragma unroll
-            for (int o = 0; o < DSEG; ++o) acc[o] = 0.f;
-#pragma unroll
-            for (int t = 0; t < SS_W; ++t) {
-                const float wt = a.g[t];
-#pragma unroll
-                for (int o = 0; o < DSEG; ++o) acc[o] = fmaf(wt, v[o + t], acc[o]);
-            }
-            float *dst = dh + k * G::HM_PLANE + r * G::MP + c0;
-#pragma unroll
-            for (int o = 0; o < DSEG; ++o) dst[o] = acc[o];
-        }
-        __syncthreads();
-        // ---- vertical pass (SS_T x SS_T), 8 outputs per item, into the
-        // D planes (free now)
-        float *gv = dmap;
-        constexpr int VSEG = 8, VNS = SS_T / VSEG;
-        for (int it = threadIdx.x; it < 3 * SS_T * VNS; it += SS_THREADS) {
-            const int cx = it % SS_T, rest = it / SS_T;
-            const int r0 = (rest % VNS) * VSEG, k = rest / VNS;
-            const float *src = dh + k * G::HM_PLANE + r0 * G::MP + cx;
-            float v[VSEG + 2 * SS_R];
-#pragma unroll
-            for (int j = 0; j < VSEG + 2 * SS_R; ++j) v[j] = src[j * G::MP];
-#pragma unroll
-            for (int o = 0; o < VSEG; ++o) {
-                float acc = 0.f;
-#pragma unroll
-                for (int t = 0; t < SS_W; ++t) acc = fmaf(a.g[t], v[o + t], acc);
-                gv[k * G::HM_PLANE + (r0 + o) * G::MP + cx] = acc;
-            }
-        }
-        __syncthreads();
-        // ---- gradient and the L1 term at the tile's pixels
-        float *D = a.grad + img * a.ds[0] + ch * a.ds[1];
-        for (int i = threadIdx.x; i < SS_T * SS_T; i += SS_THREADS) {
-            const int r = i / SS_T, cx = i % SS_T;
-            const int gy = y0 + r, gx = x0 + cx;
-            if (gy >= a.h || gx >= a.w) continue;
-            const int o = (r + G::OFF) * G::IP + cx + G::OFF;
-            const float xv = in[o], yv = in[G::IN_PLANE + o];
-            const float d = xv - yv;
-            l1_sum += fabsf(d);
-            const float s0 = gv[r * G::MP + cx], s1 = gv[G::HM_PLANE + r * G::MP + cx],
-                        s2 = gv[2 * G::HM_PLANE + r * G::MP + cx];
-            const float sg = d > 0.f ? 1.f : (d < 0.f ? -1.f : 0.f);
-            D[gy * a.ds[2] + gx * a.ds[3]] =
-                fmaf(a.gb, fmaf(2.f * xv, s1, fmaf(yv, s2, s0)), a.ga * sg);
-        }
-    } else {
-        for (int i = threadIdx.x; i < SS_T * SS_T; i += SS_THREADS) {
-            const int r = i / SS_T, cx = i % SS_T;
-            if (y0 + r >= a.h || x0 + cx >= a.w) continue;
-            const int o = (r + G::OFF) * G::IP + cx + G::OFF;
-            l1_sum += fabsf(in[o] - in[G::IN_PLANE + o]);
-        }
-    }
-
-    // ---- loss: per-CTA partials, reduced by the last CTA in a fixed order
+    __shared__ double dred[2][SS_THREADS / 32];
     const float bs = block_sum(ssim_sum, red);
     const float bl = block_sum(l1_sum, red);
     const unsigned cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
@@ -287,7 +132,6 @@ __global__ void __launch_bounds__(SS_THREADS, 2) ssim_kernel(const SsimArgs a) {
         s += (double)__ldcg(a.partials + 2 * i);
         l += (double)__ldcg(a.partials + 2 * i + 1);
     }
-    __shared__ double dred[2][SS_THREADS / 32];
     for (int o = 16; o > 0; o >>= 1) {
         s += __shfl_xor_sync(0xffffffffu, s, o);
         l += __shfl_xor_sync(0xffffffffu, l, o);
@@ -311,14 +155,214 @@ __global__ void __launch_bounds__(SS_THREADS, 2) ssim_kernel(const SsimArgs a) {
     }
 }
 
-template <bool GRAD> void set_smem() {
-    static bool done = false;
-    if (!done) {
-        cudaFuncSetAttribute(ssim_kernel<GRAD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)Geom<GRAD>::BYTES);
-        done = true;
+template <bool GRAD>
+__global__ void __launch_bounds__(SS_THREADS, 4) ssim_map_kernel(const SsimArgs a) {
+    __shared__ float2 sxy[SS_IN * SS_IP];          // (x, y) over tile + halo
+    __shared__ float2 hA[SS_IN * SS_HP];           // horizontal (E x, E y)
+    __shared__ float2 hB[SS_IN * SS_HP];           // horizontal (E x^2, E y^2)
+    __shared__ float hP[SS_IN * SS_HP];            // horizontal E xy
+    const int plane = blockIdx.z;
+    const int img = plane / a.c, ch = plane % a.c;
+    const int y0 = blockIdx.y * SS_T, x0 = blockIdx.x * SS_T;
+    const float *X = a.img + img * a.is[0] + ch * a.is[1];
+    const float *Y = a.gt + img * a.gs[0] + ch * a.gs[1];
+    float g[SS_W];
+#pragma unroll
+    for (int t = 0; t < SS_W; ++t) g[t] = a.g[t];
+
+    // ---- tile and halo of the image and the target (zero outside), as
+    // asynchronous copies into the x and y halves of the pairs
+#pragma unroll
+    for (int k = 0; k < SS_LOADS; ++k) {
+        const int i = threadIdx.x + k * SS_THREADS;
+        if (i < SS_IN * SS_IN) {
+            const int r = i / SS_IN, cc = i - r * SS_IN;
+            const int gy = y0 - SS_R + r, gx = x0 - SS_R + cc;
+            const bool in = gy >= 0 && gy < a.h && gx >= 0 && gx < a.w;
+            const int64_t ox = in ? gy * a.is[2] + gx * a.is[3] : 0;
+            const int64_t oy = in ? gy * a.gs[2] + gx * a.gs[3] : 0;
+            float *d = reinterpret_cast<float *>(&sxy[r * SS_IP + cc]);
+            cp_async<4>(d, X + ox, in);
+            cp_async<4>(d + 1, Y + oy, in);
+        }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+
+    // ---- horizontal pass: (row, 4 outputs) per item; x and y (then x^2
+    // and y^2) share packed FMAs, xy runs scalar
+    for (int it = threadIdx.x; it < SS_IN * (SS_T / 4); it += SS_THREADS) {
+        const int r = it % SS_IN, c0 = (it / SS_IN) * 4;
+        float2 v[14], acc2[4];
+        float p[14], acc[4];
+#pragma unroll
+        for (int j = 0; j < 14; ++j) {
+            v[j] = sxy[r * SS_IP + c0 + j];
+            p[j] = v[j].x * v[j].y;
+        }
+        const int o0 = r * SS_HP + c0;
+        taps4x2(g, v, acc2);
+#pragma unroll
+        for (int o = 0; o < 4; ++o) hA[o0 + o] = acc2[o];
+        taps4(g, p, acc);
+#pragma unroll
+        for (int o = 0; o < 4; ++o) hP[o0 + o] = acc[o];
+#pragma unroll
+        for (int j = 0; j < 14; ++j) v[j] = __fmul2_rn(v[j], v[j]);
+        taps4x2(g, v, acc2);
+#pragma unroll
+        for (int o = 0; o < 4; ++o) hB[o0 + o] = acc2[o];
+    }
+    __syncthreads();
+
+    // ---- vertical pass, map, derivatives: (column, 4 rows) per thread
+    float ssim_sum = 0.f;
+    {
+        const int cx = threadIdx.x % SS_T, r0 = (threadIdx.x / SS_T) * 4;
+        float2 mA[4], mB[4];
+        float mP[4];
+        {
+            float2 v[14];
+#pragma unroll
+            for (int j = 0; j < 14; ++j) v[j] = hA[(r0 + j) * SS_HP + cx];
+            taps4x2(g, v, mA);
+#pragma unroll
+            for (int j = 0; j < 14; ++j) v[j] = hB[(r0 + j) * SS_HP + cx];
+            taps4x2(g, v, mB);
+            float q[14];
+#pragma unroll
+            for (int j = 0; j < 14; ++j) q[j] = hP[(r0 + j) * SS_HP + cx];
+            taps4(g, q, mP);
+        }
+        const int gx = x0 + cx;
+        const int64_t hw = (int64_t)a.h * a.w;
+#pragma unroll
+        for (int o = 0; o < 4; ++o) {
+            const int gy = y0 + r0 + o;
+            const bool inside = gy < a.h && gx < a.w;
+            bool counted = inside;
+            if (a.valid)
+                counted = counted && gy >= SS_R && gy < a.h - SS_R && gx >= SS_R && gx < a.w - SS_R;
+            const float mx = mA[o].x, my = mA[o].y;
+            const float mxx = mx * mx, myy = my * my, mxy = mx * my;
+            const float vx = mB[o].x - mxx, vy = mB[o].y - myy, cxy = mP[o] - mxy;
+            const float A1 = 2.f * mxy + a.c1, A2 = 2.f * cxy + a.c2;
+            const float B1 = mxx + myy + a.c1, B2 = vx + vy + a.c2;
+            const float s = (A1 * A2) / (B1 * B2);
+            if (counted) ssim_sum += s;
+            if (GRAD && inside) {
+                float d0 = 0.f, d1 = 0.f, d2 = 0.f;
+                if (counted) {
+                    const float iB1 = 1.f / B1, iB2 = 1.f / B2, iBB = iB1 * iB2;
+                    d0 = 2.f * my * (A2 - A1) * iBB - 2.f * mx * s * (iB1 - iB2);
+                    d1 = -s * iB2;
+                    d2 = 2.f * A1 * iBB;
+                }
+                const int64_t at = (int64_t)plane * hw + (int64_t)gy * a.w + gx;
+                a.dmap0[at] = d0;
+                a.dmap12[at] = make_float2(d1, d2);
+            }
+        }
+    }
+    // ---- L1 over the tile
+    float l1_sum = 0.f;
+    for (int i = threadIdx.x; i < SS_T * SS_T; i += SS_THREADS) {
+        const int r = i / SS_T, cx = i % SS_T;
+        if (y0 + r >= a.h || x0 + cx >= a.w) continue;
+        const float2 v = sxy[(r + SS_R) * SS_IP + cx + SS_R];
+        l1_sum += fabsf(v.x - v.y);
+    }
+    finish_loss(a, ssim_sum, l1_sum);
+}
+
+__global__ void __launch_bounds__(SS_THREADS, 4) ssim_grad_kernel(const SsimArgs a) {
+    __shared__ float2 s12[SS_IN * SS_IP];  // (D1, D2) over tile + halo
+    __shared__ float s0[SS_IN * SS_IP];    // D0
+    __shared__ float2 h12[SS_IN * SS_HP];  // horizontal pass of (D1, D2)
+    __shared__ float h0[SS_IN * SS_HP];
+    // tiles in the reverse of the map kernel's order: the derivative planes
+    // it wrote last are the likeliest to still be in L2
+    const int plane = gridDim.z - 1 - blockIdx.z;
+    const int img = plane / a.c, ch = plane % a.c;
+    const int y0 = (gridDim.y - 1 - blockIdx.y) * SS_T, x0 = (gridDim.x - 1 - blockIdx.x) * SS_T;
+    const int64_t hw = (int64_t)a.h * a.w;
+    const float *D0 = a.dmap0 + (int64_t)plane * hw;
+    const float2 *D12 = a.dmap12 + (int64_t)plane * hw;
+    float g[SS_W];
+#pragma unroll
+    for (int t = 0; t < SS_W; ++t) g[t] = a.g[t];
+
+    // ---- the derivative planes over the tile and halo (zero outside), as
+    // asynchronous copies
+#pragma unroll
+    for (int k = 0; k < SS_LOADS; ++k) {
+        const int i = threadIdx.x + k * SS_THREADS;
+        if (i < SS_IN * SS_IN) {
+            const int r = i / SS_IN, cc = i - r * SS_IN;
+            const int gy = y0 - SS_R + r, gx = x0 - SS_R + cc;
+            const bool in = gy >= 0 && gy < a.h && gx >= 0 && gx < a.w;
+            const int64_t at = in ? (int64_t)gy * a.w + gx : 0;
+            cp_async<8>(&s12[r * SS_IP + cc], D12 + at, in);
+            cp_async<4>(&s0[r * SS_IP + cc], D0 + at, in);
+        }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    // ---- horizontal pass: (row, 4 outputs) per item, D1 and D2 packed
+    for (int it = threadIdx.x; it < SS_IN * (SS_T / 4); it += SS_THREADS) {
+        const int r = it % SS_IN, c0 = (it / SS_IN) * 4;
+        {
+            float2 v[14], acc2[4];
+#pragma unroll
+            for (int j = 0; j < 14; ++j) v[j] = s12[r * SS_IP + c0 + j];
+            taps4x2(g, v, acc2);
+#pragma unroll
+            for (int o = 0; o < 4; ++o) h12[r * SS_HP + c0 + o] = acc2[o];
+        }
+        {
+            float q[14], acc[4];
+#pragma unroll
+            for (int j = 0; j < 14; ++j) q[j] = s0[r * SS_IP + c0 + j];
+            taps4(g, q, acc);
+#pragma unroll
+            for (int o = 0; o < 4; ++o) h0[r * SS_HP + c0 + o] = acc[o];
+        }
+    }
+    __syncthreads();
+    // ---- vertical pass and the gradient: (column, 4 rows) per thread
+    const int cx = threadIdx.x % SS_T, r0 = (threadIdx.x / SS_T) * 4;
+    float2 G12[4];
+    float G0[4];
+    {
+        float2 v[14];
+#pragma unroll
+        for (int j = 0; j < 14; ++j) v[j] = h12[(r0 + j) * SS_HP + cx];
+        taps4x2(g, v, G12);
+    }
+    {
+        float q[14];
+#pragma unroll
+        for (int j = 0; j < 14; ++j) q[j] = h0[(r0 + j) * SS_HP + cx];
+        taps4(g, q, G0);
+    }
+    const float *X = a.img + img * a.is[0] + ch * a.is[1];
+    const float *Y = a.gt + img * a.gs[0] + ch * a.gs[1];
+    float *Gd = a.grad + img * a.ds[0] + ch * a.ds[1];
+    const int gx = x0 + cx;
+#pragma unroll
+    for (int o = 0; o < 4; ++o) {
+        const int gy = y0 + r0 + o;
+        if (gy >= a.h || gx >= a.w) continue;
+        const float xv = __ldg(X + gy * a.is[2] + gx * a.is[3]);
+        const float yv = __ldg(Y + gy * a.gs[2] + gx * a.gs[3]);
+        const float d = xv - yv;
+        const float sg = d > 0.f ? 1.f : (d < 0.f ? -1.f : 0.f);
+        Gd[gy * a.ds[2] + gx * a.ds[3]] =
+            fmaf(a.gb, fmaf(2.f * xv, G12[o].x, fmaf(yv, G12[o].y, G0[o])), a.ga * sg);
     }
 }
+
+size_t ws_header() { return 256; }
 
 } // namespace
 } // namespace ubs
@@ -329,10 +373,12 @@ extern "C" {
 
 size_t ubs_ssim_workspace_bytes(int32_t n_images, int32_t channels, int32_t height,
                                 int32_t width) {
-    if (n_images <= 0 || channels <= 0 || height <= 0 || width <= 0) return 256;
+    if (n_images <= 0 || channels <= 0 || height <= 0 || width <= 0) return ws_header();
     const size_t ctas = (size_t)n_images * channels * ((height + SS_T - 1) / SS_T) *
                         ((width + SS_T - 1) / SS_T);
-    return 256 + ctas * 2 * sizeof(float);
+    const size_t part = (ctas * 2 * sizeof(float) + 255) & ~(size_t)255;
+    const size_t maps = (size_t)3 * n_images * channels * height * width * sizeof(float);
+    return ws_header() + part + maps;
 }
 
 int ubs_ssim_loss(const float *img, const int64_t *img_strides, const float *gt,
@@ -388,21 +434,25 @@ int ubs_ssim_loss(const float *img, const int64_t *img_strides, const float *gt,
         tot += gs[i];
     }
     for (int i = 0; i < SS_W; ++i) a.g[i] = (float)(gs[i] / tot);
+    const size_t ctas = (size_t)n_images * channels * a.tiles_x * a.tiles_y;
     a.counter = static_cast<unsigned *>(workspace);
-    a.partials = reinterpret_cast<float *>(static_cast<char *>(workspace) + 256);
+    a.partials = reinterpret_cast<float *>(static_cast<char *>(workspace) + ws_header());
+    char *maps = static_cast<char *>(workspace) + ws_header() +
+                 ((ctas * 2 * sizeof(float) + 255) & ~(size_t)255);
+    const size_t px_all = (size_t)n_images * channels * height * width;
+    a.dmap12 = reinterpret_cast<float2 *>(maps);
+    a.dmap0 = reinterpret_cast<float *>(maps + px_all * sizeof(float2));
     a.out = out;
     const dim3 grid(a.tiles_x, a.tiles_y, n_images * channels);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (grad) {
-        set_smem<true>();
-        UBS_TIMED("ssim_loss_grad", st,
-                  ssim_kernel<true><<<grid, SS_THREADS, Geom<true>::BYTES, st>>>(a));
+        UBS_TIMED("ssim_map", st, ssim_map_kernel<true><<<grid, SS_THREADS, 0, st>>>(a));
+        UBS_TIMED("ssim_grad", st, ssim_grad_kernel<<<grid, SS_THREADS, 0, st>>>(a));
+        note_launch(2);
     } else {
-        set_smem<false>();
-        UBS_TIMED("ssim_loss", st,
-                  ssim_kernel<false><<<grid, SS_THREADS, Geom<false>::BYTES, st>>>(a));
+        UBS_TIMED("ssim_map", st, ssim_map_kernel<false><<<grid, SS_THREADS, 0, st>>>(a));
+        note_launch();
     }
-    note_launch();
     return check_launch("ssim_loss");
 }
 

@@ -50,8 +50,11 @@ def _launch(img, gt, grad, channels_last, valid, weights):
     sd = _dims(grad, channels_last)[1] if grad is not None else None
     dev = img.device
     out = torch.empty(3, dtype=torch.float32, device=dev)
-    ws = torch.zeros(int(L.query("ubs_ssim_workspace_bytes", n, c, h, w)), dtype=torch.uint8,
+    # the ticket counter (first bytes) must start at zero; the rest is written
+    # before it is read
+    ws = torch.empty(int(L.query("ubs_ssim_workspace_bytes", n, c, h, w)), dtype=torch.uint8,
                      device=dev)
+    ws[:256].zero_()
     arr = lambda s: (ctypes.c_int64 * 4)(*s)  # noqa: E731
     si_c, sg_c = arr(si), arr(sg)
     sd_c = arr(sd) if sd is not None else None
