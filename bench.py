@@ -461,7 +461,8 @@ def bench_scene_file(p, dev, reps=3):
     import tempfile
     import time
     from ubs import ply
-    path = os.path.join(tempfile.gettempdir(), "ubs_bench_scene.ply")
+    path = os.path.join(tempfile.gettempdir(), "ubs_bench_scene_%d_%d.ply" % (
+        os.getpid(), int(os.environ.get("RANK", "0"))))
     names = ("xyz", "mean", "rgb", "opacity", "beta", "scale", "l_triangle")
 
     def ref_load():
