@@ -1175,6 +1175,17 @@ def main():
             gs2.replay()
         it_ms = time_steps(gs2.replay, K2, dev, flush)
         gs2.check()
+        # the Adam launch alone (eager, the same optimizer and gradients)
+        L.profile_start(64)
+        for _ in range(10):
+            flush.fill_(2.0)
+            gs2.optimizer.step()
+        torch.cuda.synchronize()
+        adam_prof = L.profile_stop()
+        n_ad, t_ad = adam_prof.get("adam", (0, 0.0))
+        adam_ms = t_ad / max(1, n_ad)
+        adam_bytes = sum(v.numel() for v in p2.values()) * 28  # p, g, m, v read; p, m, v written
+        adam_gbs = adam_bytes / (adam_ms * 1e-3) / 1e9 if adam_ms else None
         p3 = {k: torch.nn.Parameter(v.detach().clone()) for k, v in p.items()}
         groups3 = [{"params": [p3[k]], "lr": lr, "name": k} for k, lr in TRAIN_LRS.items()]
         adam3 = torch.optim.Adam(groups3, lr=0.0, eps=1e-15)
@@ -1189,7 +1200,17 @@ def main():
             torch_adam_iter()
         it3_ms = time_steps(torch_adam_iter, K2, dev, flush)
         fz3.renderer._check_pending()
+        hbm_peak = None
+        try:
+            hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs")
+        except (OSError, ValueError):
+            pass
         train_iter = {"value": 1000.0 / it_ms, "unit": "it/s", "ms_per_step": it_ms,
+                      "adam": {"kernel_ms": adam_ms, "bytes": adam_bytes, "achieved_gbs": adam_gbs,
+                               "frac_of_hbm": adam_gbs / hbm_peak if (adam_gbs and hbm_peak)
+                               else None,
+                               "what": "one FusedAdam launch over the 35 floats per primitive "
+                                       "of the 7 groups, 28 B per element (HBM bound)"},
                       "what": "render + the reference's training loss 0.8 L1 + 0.2 (1 - SSIM) "
                               "(one fused loss kernel) + backward + Adam update of the 7 "
                               "parameter groups (FusedAdam, one kernel), as one CUDA graph",

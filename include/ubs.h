@@ -239,13 +239,14 @@ int ubs_raster_bwd_packed(int32_t C, int64_t N, int32_t channels, int64_t n_isec
  * 1 - beta1 and 1 - beta2 are passed as the caller rounds them (torch forms
  * them in double before rounding to float).
  * The table (device memory, ubs_adam_table_bytes) lists the tensors; fill a
- * host copy with ubs_adam_table_entry and copy it to the device. */
+ * host copy with ubs_adam_table_entry and copy it to the device.  max_numel
+ * and total_numel are the largest and the summed element counts. */
 size_t ubs_adam_table_bytes(int32_t n_tensors);
 int ubs_adam_table_entry(void *host_table, int32_t index, float *param, const float *grad,
                          float *exp_avg, float *exp_avg_sq, int64_t numel, int32_t group);
 int ubs_adam_step(int32_t n_tensors, const void *device_table, const float *device_hyper,
-                  int64_t max_numel, float one_minus_beta1, float beta2, float one_minus_beta2,
-                  float eps, void *stream);
+                  int64_t max_numel, int64_t total_numel, float one_minus_beta1, float beta2,
+                  float one_minus_beta2, float eps, void *stream);
 
 /* ----------------------------------------------------------------- loss ---
  * The training loss  weight_l1 * mean|img - gt| + weight_ssim * mean(SSIM map)

@@ -143,3 +143,38 @@ def test_graphed_step_with_fused_adam_matches_eager_training():
     torch.cuda.synchronize()
     for k in pa:
         assert rel(pb[k].data, pa[k].data) < 1e-5, k
+
+
+@pytest.mark.parametrize("n_tensors", [5, 80])
+def test_ragged_unaligned_and_many_tensors(n_tensors):
+    """Odd sizes (scalar tails), parameters that are views 4 bytes into their
+    storage (no 16-byte accesses), and more tensors than the flattened
+    launch takes (the per-tensor grid)."""
+    g = torch.Generator(device=DEV).manual_seed(3)
+    sizes = [(i * 7919) % 20011 + 1 for i in range(n_tensors)]
+    pa, pb = [], []
+    for i, n in enumerate(sizes):
+        base = torch.randn(n + 1, generator=g, device=DEV)
+        if i % 2:  # a view one float into its storage
+            a = torch.nn.Parameter(base.clone()[1:])
+            b = torch.nn.Parameter(base.clone()[1:])
+        else:
+            a = torch.nn.Parameter(base[:n].clone())
+            b = torch.nn.Parameter(base[:n].clone())
+        pa.append(a)
+        pb.append(b)
+    ga = [{"params": [p], "lr": 1e-3 * (1 + i % 3)} for i, p in enumerate(pa)]
+    gb = [{"params": [p], "lr": 1e-3 * (1 + i % 3)} for i, p in enumerate(pb)]
+    ref = torch.optim.Adam(ga, lr=0.0, eps=1e-15)
+    ours = FusedAdam(gb, lr=0.0, eps=1e-15)
+    for it in range(4):
+        for a, b in zip(pa, pb):
+            grad = torch.randn(a.shape, generator=g, device=DEV)
+            a.grad = grad.clone()
+            b.grad = grad.clone()
+        ref.step()
+        ours.step()
+    torch.cuda.synchronize()
+    for a, b in zip(pa, pb):
+        assert rel(b.data, a.data) < 1e-6
+        assert rel(ours.state[b]["exp_avg_sq"], ref.state[a]["exp_avg_sq"]) < 1e-6

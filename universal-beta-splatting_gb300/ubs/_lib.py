@@ -76,7 +76,7 @@ SIGNATURES = {
                             ctypes.POINTER(ctypes.c_double)], _INT),
     "ubs_adam_table_bytes": ([_I32], _SZ),
     "ubs_adam_table_entry": ([_P, _I32, _P, _P, _P, _P, _I64, _I32], _INT),
-    "ubs_adam_step": ([_I32, _P, _P, _I64, _F, _F, _F, _F, _P], _INT),
+    "ubs_adam_step": ([_I32, _P, _P, _I64, _I64, _F, _F, _F, _F, _P], _INT),
     "ubs_quantile_mask_workspace_bytes": ([], _SZ),
     "ubs_quantile_mask": ([_I64, _I32, _P, _P, _P, _P, _P, _SZ, _P], _INT),
     "ubs_quantile_mask_bounds": ([_P, _I32, _P, _P], _INT),

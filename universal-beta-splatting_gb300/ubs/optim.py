@@ -82,6 +82,7 @@ class FusedAdam(torch.optim.Optimizer):
         self._hyper_events = [None, None]
         self._entries = active
         self._max_numel = max(p.numel() for p, _ in active)
+        self._total_numel = sum(p.numel() for p, _ in active)
         self._key = key
 
     # ----------------------------------------------------------------- step
@@ -125,7 +126,8 @@ class FusedAdam(torch.optim.Optimizer):
                for _, g in self._entries):
             raise ValueError("FusedAdam: all groups must share betas and eps")
         L.call("ubs_adam_step", len(self._entries), L.ptr(self._table_dev),
-               L.ptr(self._hyper_dev), int(self._max_numel), float(1 - b1), float(b2),
+               L.ptr(self._hyper_dev), int(self._max_numel), int(self._total_numel),
+               float(1 - b1), float(b2),
                float(1 - b2), float(group["eps"]), L.stream(self._table_dev.device))
 
     @torch.no_grad()
