@@ -196,6 +196,13 @@ def gpu_step(p, cam, ri, rj, bg, target):
 _SSIM_WIN = {}
 
 
+def l1_loss(x, y):
+    """The L1 term of the step through this library (one launch with its
+    gradient, ubs.loss.l1_loss)."""
+    from ubs.loss import l1_loss as _l1
+    return _l1(x, y)
+
+
 def torch_l1_ssim(img, gt, lam=LAMBDA_DSSIM):
     """train.py:117-121's loss on [N, 3, H, W] images with SSIM as
     utils/loss_utils.py:26-80 formulates it in PyTorch (F.conv2d, 11 x 11
@@ -246,7 +253,7 @@ class FusedStep:
             v.grad = None
         colors, _ = self.renderer.render(self.p, self.views, self.bg, check=False)
         if self.loss == "l1":
-            loss = (colors - self.target).abs().mean()
+            loss = l1_loss(colors, self.target)
         else:
             img = colors.view(1, self.hw[0], self.hw[1], 3).permute(0, 3, 1, 2)
             loss = torch_l1_ssim(img, self.target_nchw)
@@ -702,7 +709,7 @@ class TrainViews:
         for v in self.p.values():
             v.grad = None
         colors, _ = self.r.render(self.p, self.views, self.bg, check=False)
-        (colors - self.target).abs().mean().backward()
+        l1_loss(colors, self.target).backward()
 
 
 def _train_views(p, cams, dev, tile, reps, flush):
@@ -1058,7 +1065,7 @@ def main():
     g_ren = Renderer(dim=DIM, tile_size=TILE)
     prof_slots = 64 * 4
     gs = GraphedStep(g_ren, p, fz.views, fz.bg,
-                     lambda colors, alphas: (colors - g_target).abs().mean(),
+                     lambda colors, alphas: l1_loss(colors, g_target),
                      before_capture=lambda: L.profile_start(prof_slots))
     if args.profile:
         L.profile_stop()
@@ -1122,7 +1129,7 @@ def main():
     def make_inputs():
         q = {k: torch.nn.Parameter(v.detach().clone()) for k, v in p.items()}
         t = g_target.clone()
-        return q, [q[k] for k in p] + [t], lambda c, a: (c - t).abs().mean()
+        return q, [q[k] for k in p] + [t], lambda c, a: l1_loss(c, t)
 
     hf = HostFedStep(Renderer(dim=DIM, tile_size=TILE), fz.views, fz.bg, make_inputs)
     feed_host = [host[k] for k in p] + [host_target]

@@ -276,6 +276,14 @@ int ubs_ssim_loss(const float *img, const int64_t *img_strides, const float *gt,
                   double weight_const, float *out, void *workspace, size_t workspace_bytes,
                   void *stream);
 
+/* The L1 term alone (utils/loss_utils.py:18-19, train.py:117): out[0] =
+ * mean |x - y| over n contiguous floats, out[1] = weight out[0], and (grad
+ * != NULL) grad = weight sign(x - y) / n, in one launch.  Workspace as for
+ * ubs_ssim_loss: the first 256 bytes zero before first use, left zero. */
+size_t ubs_l1_loss_workspace_bytes(int64_t n);
+int ubs_l1_loss(const float *x, const float *y, float *grad, int64_t n, double weight,
+                float *out, void *workspace, size_t workspace_bytes, void *stream);
+
 /* --------------------------------------------------- MCMC densification ---
  * BetaModel.relocate_gs / add_new_gs (scene/beta_model.py:553-658) and the
  * position noise of train.py:164-171, on the device with no host

@@ -170,3 +170,18 @@ def test_errors():
         LS.ssim(a.double(), a.double())
     with pytest.raises(ValueError):
         LS.ssim(a, a, padding="full")
+
+
+@pytest.mark.parametrize("n", [1, 7, 4096, 6_220_803])
+def test_l1_loss_matches_torch(n):
+    g = torch.Generator().manual_seed(n)
+    x = torch.rand(n, generator=g).to(DEV).requires_grad_(True)
+    y = torch.rand(n, generator=g).to(DEV)
+    y[: n // 3] = x.detach()[: n // 3]  # ties: the gradient is 0 there, as torch's sign
+    l = LS.l1_loss(x, y)
+    (2.0 * l).backward()
+    xr = x.detach().clone().requires_grad_(True)
+    lr = (xr - y).abs().mean()
+    (2.0 * lr).backward()
+    assert abs(l.item() - lr.item()) <= 1e-6 * abs(lr.item())
+    assert torch.equal(x.grad, xr.grad)

@@ -362,6 +362,77 @@ __global__ void __launch_bounds__(SS_THREADS, 4) ssim_grad_kernel(const SsimArgs
     }
 }
 
+// ---- L1 alone (train.py's l1_loss, utils/loss_utils.py:18-19): mean |x - y|
+// over contiguous arrays and its gradient sign(x - y) w / n, one pass; the
+// sums reduced like the SSIM partials (fixed order, last CTA).
+constexpr int L1_THREADS = 256;
+constexpr int L1_PER = 8; // float4 per thread per pass
+
+__global__ void __launch_bounds__(L1_THREADS) l1_kernel(const float *__restrict__ x,
+                                                        const float *__restrict__ y,
+                                                        float *__restrict__ grad, int64_t n,
+                                                        float gscale, double inv_n, double w,
+                                                        float *partials, unsigned *counter,
+                                                        float *out) {
+    float acc = 0.f;
+    const int64_t n4 = n >> 2;
+    const bool vec = ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y) |
+                       reinterpret_cast<uintptr_t>(grad)) & 15) == 0;
+    const int64_t stride = (int64_t)gridDim.x * L1_THREADS;
+    if (vec) {
+        for (int64_t i = (int64_t)blockIdx.x * L1_THREADS + threadIdx.x; i < n4; i += stride) {
+            const float4 a = reinterpret_cast<const float4 *>(x)[i];
+            const float4 b = reinterpret_cast<const float4 *>(y)[i];
+            const float d0 = a.x - b.x, d1 = a.y - b.y, d2 = a.z - b.z, d3 = a.w - b.w;
+            acc += fabsf(d0) + fabsf(d1) + fabsf(d2) + fabsf(d3);
+            if (grad) {
+                auto sg = [](float d) { return d > 0.f ? 1.f : (d < 0.f ? -1.f : 0.f); };
+                reinterpret_cast<float4 *>(grad)[i] = make_float4(
+                    gscale * sg(d0), gscale * sg(d1), gscale * sg(d2), gscale * sg(d3));
+            }
+        }
+    }
+    for (int64_t i = (vec ? n4 * 4 : 0) + (int64_t)blockIdx.x * L1_THREADS + threadIdx.x; i < n;
+         i += stride) {
+        const float d = x[i] - y[i];
+        acc += fabsf(d);
+        if (grad) grad[i] = gscale * (d > 0.f ? 1.f : (d < 0.f ? -1.f : 0.f));
+    }
+    __shared__ float red[L1_THREADS / 32];
+    __shared__ bool last;
+    __shared__ double dred[L1_THREADS / 32];
+    const float bs = block_sum(acc, red);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = bs;
+        __threadfence();
+        last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double s = 0.0;
+    for (unsigned i = threadIdx.x; i < gridDim.x; i += L1_THREADS) s += (double)__ldcg(partials + i);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) dred[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int i = 0; i < L1_THREADS / 32; ++i) t += dred[i];
+        out[0] = (float)(t * inv_n);
+        out[1] = (float)(w * t * inv_n);
+        *counter = 0u;
+    }
+}
+
+int l1_grid(int64_t n) {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t want = (n / 4 + (int64_t)L1_THREADS * L1_PER - 1) / ((int64_t)L1_THREADS * L1_PER);
+    const int64_t cap = (int64_t)sms * 8;
+    return (int)(want < 1 ? 1 : (want < cap ? want : cap));
+}
+
 size_t ws_header() { return 256; }
 
 } // namespace
@@ -454,6 +525,28 @@ int ubs_ssim_loss(const float *img, const int64_t *img_strides, const float *gt,
         note_launch();
     }
     return check_launch("ssim_loss");
+}
+
+size_t ubs_l1_loss_workspace_bytes(int64_t n) {
+    return ws_header() + (((size_t)l1_grid(n < 1 ? 1 : n) * sizeof(float) + 255) & ~(size_t)255);
+}
+
+int ubs_l1_loss(const float *x, const float *y, float *grad, int64_t n, double weight,
+                float *out, void *workspace, size_t workspace_bytes, void *stream) {
+    UBS_REQUIRE(n > 0 && x && y && out, "l1_loss: bad arguments");
+    UBS_REQUIRE(workspace && workspace_bytes >= ubs_l1_loss_workspace_bytes(n),
+                "l1_loss: workspace too small");
+    const int grid = l1_grid(n);
+    unsigned *counter = static_cast<unsigned *>(workspace);
+    float *partials = reinterpret_cast<float *>(static_cast<char *>(workspace) + ws_header());
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // d mean / d x as torch forms it: the mean's 1/n in float, times the weight
+    const float gscale = (float)weight * (float)(1.0 / (double)n);
+    UBS_TIMED("l1_loss", st,
+              l1_kernel<<<grid, L1_THREADS, 0, st>>>(x, y, grad, n, gscale, 1.0 / (double)n,
+                                                     weight, partials, counter, out));
+    note_launch();
+    return check_launch("l1_loss");
 }
 
 } // extern "C"

@@ -92,6 +92,8 @@ SIGNATURES = {
     "ubs_mcmc_add": ([_P, _P, _I64, _I64, ctypes.c_uint64, _P, _P, _P, _SZ, _P], _INT),
     "ubs_mcmc_perturb_xyz": ([_I64, _I32, _P, _P, _P, _P, _F, ctypes.c_uint64, _P, _P], _INT),
     "ubs_ssim_workspace_bytes": ([_I32, _I32, _I32, _I32], _SZ),
+    "ubs_l1_loss_workspace_bytes": ([_I64], _SZ),
+    "ubs_l1_loss": ([_P, _P, _P, _I64, _D, _P, _P, _SZ, _P], _INT),
     "ubs_ssim_loss": ([_P, _P, _P, _P, _P, _P, _I32, _I32, _I32, _I32, _I32, _D, _D, _D, _P,
                        _P, _SZ, _P], _INT),
     "ubs_fp32_probe_workspace_bytes": ([], _SZ),

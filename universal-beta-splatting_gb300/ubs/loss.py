@@ -3,8 +3,10 @@
 train.py:117-121 trains on  (1 - l) L1(image, gt) + l (1 - SSIM(image, gt))
 (l = lambda_dssim, 0.2) with SSIM from the fused_ssim package, which
 evaluates utils/loss_utils.py:26-80's definition.  `l1_ssim_loss` computes
-that loss and writes d loss / d image in the same launch (the backward pass
-only scales it by the incoming gradient); `ssim` is the SSIM term alone.
+that loss and writes d loss / d image in the same launches (the backward
+pass only scales it by the incoming gradient); `ssim` is the SSIM term
+alone and `l1_loss` the L1 term alone (utils/loss_utils.py:18-19), one
+launch with its gradient.
 
 Images may be laid out as [..., C, H, W] or, with channels_last=True, as
 [..., H, W, C] (the renderer's layout) with any strides: nothing is copied.
@@ -106,3 +108,46 @@ def ssim(img, gt, channels_last=False, padding="same"):
     if padding not in ("same", "valid"):
         raise ValueError("padding must be 'same' or 'valid'")
     return _apply(img, gt, channels_last, padding == "valid", _W_SSIM_ONLY, 0)
+
+
+class _L1(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, y):
+        grad = torch.empty_like(x) if ctx.needs_input_grad[0] else None
+        out = _l1_launch(x.detach(), y.detach(), grad)
+        ctx.save_for_backward(grad)
+        return out[0]
+
+    @staticmethod
+    def backward(ctx, g):
+        (grad,) = ctx.saved_tensors
+        return grad * g, None
+
+
+def _l1_launch(x, y, grad):
+    n = x.numel()
+    dev = x.device
+    out = torch.empty(2, dtype=torch.float32, device=dev)
+    ws = torch.empty(int(L.query("ubs_l1_loss_workspace_bytes", n)), dtype=torch.uint8,
+                     device=dev)
+    ws[:256].zero_()
+    L.call("ubs_l1_loss", L.ptr(x), L.ptr(y), L.ptr(grad) if grad is not None else None, n,
+           1.0, L.ptr(out), L.ptr(ws), ws.numel(), L.stream(dev))
+    return out
+
+
+def l1_loss(img, gt):
+    """mean |img - gt| (utils/loss_utils.py:18-19) of two contiguous float32
+    CUDA tensors of one shape, differentiable w.r.t. img; one launch writes
+    the value and the gradient."""
+    if not (img.is_cuda and gt.is_cuda) or img.dtype != torch.float32 or \
+            gt.dtype != torch.float32:
+        raise TypeError("l1_loss needs float32 CUDA tensors")
+    if img.shape != gt.shape:
+        raise ValueError("shapes differ: %s vs %s" % (tuple(img.shape), tuple(gt.shape)))
+    if not (img.is_contiguous() and gt.is_contiguous()):
+        raise ValueError("l1_loss needs contiguous tensors")
+    if torch.is_grad_enabled() and img.requires_grad:
+        return _L1.apply(img, gt.detach())
+    with torch.no_grad():
+        return _l1_launch(img.detach(), gt.detach(), None)[0]
