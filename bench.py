@@ -743,6 +743,82 @@ def _ref_train_views(rp, p, cams, dev, reps, flush):
     return time_steps(step, reps, dev, flush)
 
 
+def look_at_camera(eye, width, height, focal):
+    """Camera at `eye` looking at the origin, up +y, OpenCV axes, principal
+    point at the image centre."""
+    from ubs import scene as S
+    e = torch.tensor(eye, dtype=torch.float64)
+    f = -e / e.norm()
+    r = torch.linalg.cross(f, torch.tensor([0.0, 1.0, 0.0], dtype=torch.float64))
+    r = r / r.norm()
+    u = torch.linalg.cross(r, f)
+    Rw = torch.stack([r, -u, f], 0)
+    vm = torch.eye(4, dtype=torch.float64)
+    vm[:3, :3] = Rw
+    vm[:3, 3] = -Rw @ e
+    K = torch.tensor([[focal, 0.0, width / 2], [0.0, focal, height / 2], [0.0, 0.0, 1.0]])
+    return S.Camera(vm.float(), K, width, height)
+
+
+def run_config_a(dev, flush):
+    """The reference's CPU-runnable case: 10k 6-D primitives (xyz in
+    [-1, 1]^3), 256x256, fx = fy = 300, camera at (0, 0, -3) looking at the
+    origin, L1 loss: forward and forward + backward through the oracle port
+    on the host cores (all threads, then one thread) -- a reported baseline
+    -- and through the fused GPU path on the same scene."""
+    import oracle as orc
+    from ubs.render import Renderer, Views
+    W = H = 256
+    cam = look_at_camera((0.0, 0.0, -3.0), W, H, 300.0)
+    cs = CpuSample(10_000, 0, width=W, height=H, cam=cam, xyz_range=1.0)
+
+    def cpu_times(reps=3):
+        fwd = min(cs.forward() for _ in range(reps))
+        step = min(cs.step(1, 0, 1) for _ in range(reps))
+        return {"fwd_ms": fwd * 1e3, "fwd_bwd_ms": step * 1e3}
+
+    threads = orc.num_threads()
+    cpu_all = cpu_times()
+    orc.set_threads(1)
+    try:
+        cpu_one = cpu_times()
+    finally:
+        orc.set_threads(threads)
+    p = {k: torch.from_numpy(v).to(dev).contiguous() for k, v in cs.p.items()}
+    p = {k: torch.nn.Parameter(v) for k, v in p.items()}
+    cam_d = type(cam)(cam.viewmat.to(dev), cam.K.to(dev), W, H)
+    views = Views([cam_d], tile_size=TILE, device=dev)
+    r = Renderer(dim=DIM, tile_size=TILE)
+    target = torch.from_numpy(cs.target_hwc).to(dev).reshape(-1, 3).contiguous()
+    with torch.no_grad():
+        r.render(p, views, None, check=True)
+
+    def g_fwd():
+        with torch.no_grad():
+            r.render(p, views, None, check=False)
+
+    def g_step():
+        for v in p.values():
+            v.grad = None
+        colors, _ = r.render(p, views, None, check=False)
+        l1_loss(colors, target).backward()
+
+    for _ in range(3):
+        g_step()
+    fwd_ms = time_steps(g_fwd, 50, dev, flush)
+    step_ms = time_steps(g_step, 50, dev, flush)
+    r._check_pending()
+    return {"workload": "10k 6-D primitives, 256x256 (fx=fy=300), camera at (0, 0, -3) looking "
+                        "at the origin, forward + L1 loss + backward",
+            "gpu": {"fwd_ms": fwd_ms, "fwd_bwd_ms": step_ms,
+                    "path": "fused scene render, kernel by kernel"},
+            "cpu": dict(cpu_all, threads=threads, kind="port",
+                        what="the oracle port (C++ restatement, OpenMP) on the host cores, a "
+                             "reported baseline"),
+            "cpu_1_thread": dict(cpu_one, threads=1),
+            "intersections": cs.n_isects}
+
+
 def run_config_c(dev, flush, rp):
     """500k 7-D dynamic primitives, 8 views of 1352x1014 with timestamps, one
     batched forward + backward."""
@@ -854,12 +930,13 @@ def run_serving(dev, rp, duration=3.0, rate=200.0):
 
 
 # ------------------------------------------------------- CPU (oracle port)
-def cpu_problem(n_prims, seed):
+def cpu_problem(n_prims, seed, width=WIDTH, height=HEIGHT, cam=None, xyz_range=2.0):
     from ubs import scene as S
     p = {k: v.numpy().astype(np.float32) for k, v in
-         S.synthetic_params(n_prims, DIM, seed=seed, xyz_range=2.0, device="cpu").items()}
-    cam = S.orbit_view(seed, 4.0, WIDTH, HEIGHT, FOCAL, FOCAL, device="cpu")
-    target = torch.rand(3, HEIGHT, WIDTH, generator=torch.Generator().manual_seed(seed + 7)).numpy()
+         S.synthetic_params(n_prims, DIM, seed=seed, xyz_range=xyz_range, device="cpu").items()}
+    if cam is None:
+        cam = S.orbit_view(seed, 4.0, width, height, FOCAL, FOCAL, device="cpu")
+    target = torch.rand(3, height, width, generator=torch.Generator().manual_seed(seed + 7)).numpy()
     ri, rj = S.rest_indices(DIM)
     return p, cam, ri.numpy(), rj.numpy(), target
 
@@ -876,12 +953,14 @@ class CpuSample:
     used).  Each part's time is scaled to the whole frame (x N / slice,
     x rows / sampled rows); consecutive steps cycle over slices and rows."""
 
-    def __init__(self, n_prims, seed=0):
+    def __init__(self, n_prims, seed=0, width=WIDTH, height=HEIGHT, cam=None, xyz_range=2.0):
         import oracle as orc
         self.orc = orc
-        self.p, self.cam, self.ri, self.rj, self.target = cpu_problem(n_prims, seed)
+        self.W, self.H = width, height
+        self.p, self.cam, self.ri, self.rj, self.target = cpu_problem(n_prims, seed, width,
+                                                                       height, cam, xyz_range)
         self.N = n_prims
-        self.tw, self.th = math.ceil(WIDTH / TILE), math.ceil(HEIGHT / TILE)
+        self.tw, self.th = math.ceil(width / TILE), math.ceil(height / TILE)
         t0 = time.perf_counter()
         self.full = self._prim_forward(slice(None))
         _, ids, self.fl = orc.isect_tiles(self.full["m2"], self.full["radii"], self.full["d"],
@@ -892,14 +971,14 @@ class CpuSample:
         # reused blend buffers: a sampled step writes only its rows, so that
         # no full-frame allocation or loss is scaled with the sample
         C = 1
-        self.out_f = (np.zeros((C, HEIGHT, WIDTH, 3), np.float32),
-                      np.zeros((C, HEIGHT, WIDTH, 1), np.float32),
-                      np.zeros((C, HEIGHT, WIDTH), np.int32))
+        self.out_f = (np.zeros((C, height, width, 3), np.float32),
+                      np.zeros((C, height, width, 1), np.float32),
+                      np.zeros((C, height, width), np.int32))
         self.out_b = (np.zeros((C, n_prims, 2), np.float32), np.zeros((C, n_prims, 3), np.float32),
                       np.zeros((C, n_prims, 3), np.float32), np.zeros((C, n_prims), np.float32),
                       np.zeros((C, n_prims), np.float32))
-        self.v_oc = np.zeros((C, HEIGHT, WIDTH, 3), np.float32)
-        self.v_oa = np.zeros((C, HEIGHT, WIDTH, 1), np.float32)
+        self.v_oc = np.zeros((C, height, width, 3), np.float32)
+        self.v_oa = np.zeros((C, height, width, 1), np.float32)
         self.target_hwc = np.ascontiguousarray(self.target.transpose(1, 2, 0))
 
     def _prim_forward(self, sl):
@@ -919,14 +998,15 @@ class CpuSample:
         m_nd = np.concatenate([p["xyz"][sl], p["mean"][sl]], 1)
         om, oV, oo = orc.cond_mean_convariance_opacity(m_nd, cov, opac, beta[:, 1:], q)
         c6 = np.ascontiguousarray(oV[:, [0, 0, 0, 1, 1, 2], [0, 1, 2, 1, 2, 2]])
-        radii, m2, d, cn, _ = orc.fully_fused_projection(om, c6, None, None, vm, K, WIDTH, HEIGHT)
+        radii, m2, d, cn, _ = orc.fully_fused_projection(om, c6, None, None, vm, K, self.W,
+                                                         self.H)
         return dict(sp=sp, beta=beta, opac=opac, vm=vm, K=K, q=q, R=R, cov=cov, m_nd=m_nd,
                     om=om, oV=oV, oo=oo, c6=c6, radii=radii, m2=m2, d=d, cn=cn, ltri=ltri)
 
     def _prim_backward(self, f, vm2, vcn, vo):
         orc = self.orc
         vmeans, vc6, _, _, _ = orc.fully_fused_projection_bwd(
-            f["om"], f["c6"], None, None, f["vm"], f["K"], WIDTH, HEIGHT, 0.3, f["radii"],
+            f["om"], f["c6"], None, None, f["vm"], f["K"], self.W, self.H, 0.3, f["radii"],
             f["cn"], None, vm2, None, vcn)
         v_oV = np.zeros_like(f["oV"])
         for k, (i, j) in enumerate(zip([0, 0, 0, 1, 1, 2], [0, 1, 2, 1, 2, 2])):
@@ -938,6 +1018,19 @@ class CpuSample:
                                                            self.rj, gV)
         vl[:, :3] += orc.l_triangle_to_rotmat_bwd(vr)
         return gm, vs, vl
+
+    def forward(self):
+        """Seconds of one full forward: per-primitive forward, intersection
+        sort and offsets, blend."""
+        orc = self.orc
+        t0 = time.perf_counter()
+        f = self._prim_forward(slice(None))
+        _, ids, fl = orc.isect_tiles(f["m2"], f["radii"], f["d"], TILE, self.tw, self.th)
+        offs = orc.isect_offset_encode(ids, 1, self.tw, self.th)
+        orc.rasterize_to_pixels(f["m2"], f["cn"], self.p["rgb"][None], f["oo"].reshape(1, -1),
+                                f["beta"][:, 0].reshape(1, -1), self.W, self.H, TILE, offs, fl,
+                                backgrounds=np.zeros((1, 3), np.float32))
+        return time.perf_counter() - t0
 
     def step(self, F, k, FP=None):
         """Scaled seconds of one full-frame step, sampled as described above
@@ -955,16 +1048,16 @@ class CpuSample:
         op, be = full["oo"].reshape(1, -1), full["beta"][:, 0].reshape(1, -1)
         bg = np.zeros((1, 3), np.float32)
         off = k % F
-        oc, oa, li = orc.rasterize_to_pixels(full["m2"], full["cn"], colors, op, be, WIDTH,
-                                             HEIGHT, TILE, self.offs, self.fl, backgrounds=bg,
+        oc, oa, li = orc.rasterize_to_pixels(full["m2"], full["cn"], colors, op, be, self.W,
+                                             self.H, TILE, self.offs, self.fl, backgrounds=bg,
                                              row_step=F, row_offset=off, out=self.out_f)
         # L1 loss gradient on the sampled pixel rows
         for ty in range(off, self.th, F):
-            r0, r1 = ty * TILE, min(HEIGHT, (ty + 1) * TILE)
+            r0, r1 = ty * TILE, min(self.H, (ty + 1) * TILE)
             d = oc[0, r0:r1] - self.target_hwc[r0:r1]
-            self.v_oc[0, r0:r1] = np.sign(d) / (3.0 * HEIGHT * WIDTH)
+            self.v_oc[0, r0:r1] = np.sign(d) / (3.0 * self.H * self.W)
         vm2, vcn, _, vo, _ = orc.rasterize_to_pixels_bwd(
-            full["m2"], full["cn"], colors, op, be, WIDTH, HEIGHT, TILE, self.offs, self.fl, oa,
+            full["m2"], full["cn"], colors, op, be, self.W, self.H, TILE, self.offs, self.fl, oa,
             li, self.v_oc, self.v_oa, backgrounds=bg, row_step=F, row_offset=off,
             out=self.out_b)
         t_blend = time.perf_counter() - t1
@@ -1348,7 +1441,8 @@ def main():
     if not args.no_configs and rank == 0:
         rp = _ref_pipeline() if not args.no_ref_gpu else None
         configs = {}
-        for name, fn in (("C", lambda: run_config_c(dev, flush, rp)),
+        for name, fn in (("A", lambda: run_config_a(dev, flush)),
+                         ("C", lambda: run_config_c(dev, flush, rp)),
                          ("D", lambda: run_config_d(dev, flush, rp)),
                          ("E", lambda: run_serving(dev, rp))):
             try:
