@@ -67,3 +67,24 @@ def test_realtime_trace_latency():
     done = srv.run(tr, realtime=True)
     st = latency_stats(done)
     assert st["requests"] == len(tr) and 0 < st["p50_ms"] <= st["p99_ms"] < 1000
+
+
+def test_scene_loaded_from_ply_serves_the_same_images(tmp_path):
+    """Server.load_scene (the reference's PLY file, unpacked on the device)
+    serves exactly what the same scene served from memory does."""
+    from ubs import ply
+    p = S.synthetic_params(20000, 7, seed=4, xyz_range=1.0, device=DEV)
+    p["scale"][:, :3] += 1.0
+    path = str(tmp_path / "scene.ply")
+    ply.save_ply(path, p)
+    cfg = ServeConfig(max_slots=2, max_batch_views=4, mem_budget=2 << 30, keep_images=True)
+    a = Server({"s": p}, cfg)
+    b = Server({}, cfg)
+    b.load_scene("s", path)
+    tr = poisson_trace(1000.0, 10.0, ["s"], RES, seed=6, radius=3.0, focal_per_width=0.9,
+                       device=DEV)[:8]
+    da = {d.rid: d.image for d in a.run(tr, realtime=False)}
+    db = {d.rid: d.image for d in b.run(tr, realtime=False)}
+    assert sorted(da) == sorted(db) == list(range(8))
+    for rid in da:
+        assert torch.equal(da[rid], db[rid]), rid

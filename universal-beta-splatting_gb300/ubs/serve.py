@@ -164,16 +164,31 @@ class Server:
         self.cfg = cfg or ServeConfig()
         self.device = torch.device(device)
         self.scenes = {}
+        self.ipp = {}  # intersections per pixel, per scene
         for name, p in scenes.items():
-            q = {k: p[k].detach().float().contiguous() for k in PARAM_ORDER}
-            q["opacity"] = q["opacity"].reshape(-1)
-            self.scenes[name] = q
+            self.add_scene(name, p)
         self.eps2d, self.near, self.far = eps2d, near_plane, far_plane
         self.streams = [torch.cuda.Stream(self.device) for _ in range(self.cfg.max_slots)]
         self.free_streams = list(range(self.cfg.max_slots))
-        self.ipp = {}  # intersections per pixel, per scene
         self.bg = torch.zeros(self.cfg.max_batch_views, 3, device=self.device)
         self.reruns = 0
+
+    # scenes -------------------------------------------------------------
+    def add_scene(self, name: str, params: Dict[str, torch.Tensor]):
+        """Make a scene resident: raw parameter tensors under the reference's
+        names (xyz, mean, scale, l_triangle, opacity, beta, rgb)."""
+        q = {k: params[k].detach().to(self.device, torch.float32).contiguous()
+             for k in PARAM_ORDER}
+        q["opacity"] = q["opacity"].reshape(-1)
+        self.scenes[name] = q
+        self.ipp.pop(name, None)  # a new scene is calibrated afresh
+
+    def load_scene(self, name: str, path: str):
+        """Make the scene of a reference PLY file resident (scene/beta_model.py:
+        322-404's format; the vertex records go to the device as they are and
+        are unpacked there, ubs.ply.load_ply)."""
+        from .ply import load_ply
+        self.add_scene(name, load_ply(path, self.device))
 
     # sizes --------------------------------------------------------------
     def _dim(self, scene):
