@@ -198,3 +198,56 @@ def test_fused_tile_sizes_match_dropin(ts):
     (img_f * w).sum().backward()
     for k in leaves_d:
         assert rel_l2(leaves_f[k].grad, leaves_d[k].grad) < 1e-4, k
+
+
+def test_fused_empty_scene_and_nothing_visible():
+    """No primitives, or none in front of the camera: the image is the
+    background, alphas are zero, gradients are zero, nothing overflows."""
+    bg = torch.tensor([0.25, 0.5, 0.75], device=DEV)
+    cam = S.orbit_view(1, 3.0, 64, 48, 60.0, 60.0, device=DEV)
+    empty = {k: v[:0] for k, v in make_params(10, 6, seed=1).items()}
+    r, views, colors, alphas, leaves = fused_render(empty, [cam], bg)
+    assert torch.equal(colors, bg.expand_as(colors)) and not alphas.any()
+    colors.sum().backward()  # empty gradients, no launch failure
+    p = make_params(2000, 6, seed=2)
+    with torch.no_grad():
+        center = cam.center.to(DEV)
+        fwd = torch.inverse(cam.viewmat.to(DEV))[:3, 2]
+        p["xyz"].copy_(center - 5.0 * fwd + 0.1 * torch.randn_like(p["xyz"]))  # behind it
+    r, views, colors, alphas, leaves = fused_render(p, [cam], bg)
+    assert torch.equal(colors, bg.expand_as(colors)) and not alphas.any()
+    (colors * torch.rand_like(colors)).sum().backward()
+    for k, v in leaves.items():
+        assert v.grad is not None and not v.grad.any(), k
+
+
+@pytest.mark.parametrize("W,H", [(17, 13), (1, 1), (33, 5)])
+def test_fused_odd_and_tiny_images_match_dropin(W, H):
+    """Partial tiles and single pixels: the fused path agrees with the
+    drop-in sequence image for image and gradient for gradient."""
+    p = make_params(3000, 6, seed=W + H)
+    cam = S.orbit_view(3, 3.0, W, H, 20.0 * max(W, H) / 17, 20.0 * max(W, H) / 17, device=DEV)
+    bg = torch.tensor([0.1, 0.2, 0.3], device=DEV)
+    img_d, alpha_d, leaves_d = dropin_render(p, cam, bg)
+    _, views, colors, alphas, leaves_f = fused_render(p, [cam], bg)
+    img_f = views.split(colors)[0]
+    assert img_f.shape == (H, W, 3)
+    assert float((img_f - img_d).detach().abs().max()) < 1e-5
+    g = torch.Generator().manual_seed(1)
+    w = torch.randn(H, W, 3, generator=g).to(DEV)
+    (img_d * w).sum().backward()
+    (img_f * w).sum().backward()
+    for k in leaves_d:
+        if leaves_d[k].grad.abs().max() > 0:
+            assert rel_l2(leaves_f[k].grad, leaves_d[k].grad) < 1e-4, k
+
+
+def test_fused_near_plane_culls():
+    """A near plane beyond every primitive renders the background only."""
+    p = make_params(2000, 6, seed=7)
+    cam = S.orbit_view(2, 3.0, 64, 48, 60.0, 60.0, device=DEV)
+    bg = torch.tensor([0.3, 0.3, 0.3], device=DEV)
+    r = Renderer(dim=6, near_plane=100.0)
+    with torch.no_grad():
+        colors, alphas = r.render(p, Views([cam], device=DEV), bg)
+    assert torch.equal(colors, bg.expand_as(colors)) and not alphas.any()

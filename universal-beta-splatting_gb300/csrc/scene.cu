@@ -498,8 +498,10 @@ int scene_common(SceneArgs &a, int32_t dim, int64_t N, const float *xyz, const f
     UBS_REQUIRE((int64_t)C * N < (1ll << 31), "scene: views x primitives must fit in int32");
     UBS_REQUIRE(tile_size == 8 || tile_size == 16 || tile_size == 24 || tile_size == 32,
                 "scene: tile_size %d (supported 8, 16, 24, 32)", tile_size);
-    UBS_REQUIRE(xyz && mean && scale && ltri && opac && beta && rgb && viewmats && intr &&
-                    centers && dims && tile_base && (dim == 6 || times),
+    // an empty scene (N = 0) may pass null parameter pointers: it renders the
+    // background
+    UBS_REQUIRE((N == 0 || (xyz && mean && scale && ltri && opac && beta && rgb)) && viewmats &&
+                    intr && centers && dims && tile_base && (dim == 6 || times),
                 "scene: null input pointer");
     a.N = N;
     a.C = C;
@@ -673,8 +675,9 @@ int ubs_scene_backward(int32_t dim, int64_t N, const float *xyz, const float *me
                              tile_size, eps2d, near_plane, far_plane, radius_clip))
         return e;
     UBS_REQUIRE(n_buckets >= 1 && capacity >= 1 && pix_base && render_alphas && last_ids &&
-                    v_render_colors && v_render_alphas && v_xyz && v_mean && v_scale &&
-                    v_l_triangle && v_opacity && v_beta && v_rgb,
+                    v_render_colors && v_render_alphas &&
+                    (N == 0 || (v_xyz && v_mean && v_scale && v_l_triangle && v_opacity &&
+                                v_beta && v_rgb)),
                 "scene_backward: null argument");
     UBS_REQUIRE(capacity < (1ll << 31), "scene_backward: capacity %lld exceeds 2^31 - 1",
                 (long long)capacity);
