@@ -201,3 +201,12 @@ def test_bad_given_draws():
     dead[:2] = True
     st = mcmc.relocate_gs(m, dead, src=torch.tensor([10, 999]))
     assert int(st.item()) != 0
+
+
+def test_relocate_without_live_primitives_changes_nothing():
+    """As the reference's early return: nothing to draw from."""
+    m, vals = synthetic(300, 9, dead_frac=1.0)
+    before = {k: getattr(m, "_" + k).detach().clone() for k in orc.MCMC_NAMES}
+    mcmc.relocate_gs(m, torch.ones(300, dtype=torch.bool, device=DEV))
+    for k in orc.MCMC_NAMES:
+        assert torch.equal(getattr(m, "_" + k), before[k]), k

@@ -161,3 +161,17 @@ def test_depth_to_normal_definition():
     nn /= np.linalg.norm(nn, axis=-1, keepdims=True)
     assert np.allclose(n[1:-1, 1:-1], nn, atol=1e-4)
     assert not n[0].any() and not n[-1].any() and not n[:, 0].any() and not n[:, -1].any()
+
+
+def test_empty_scene_renders_background():
+    """rasterization() of no primitives: the background, zero alpha, as the
+    reference (its kernels see empty ranges everywhere)."""
+    cam = S.orbit_view(1, 3.0, W, H, 150.0, 150.0)
+    bg = torch.tensor([[0.2, 0.4, 0.6]], device=DEV)
+    e3 = torch.zeros(0, 3, device=DEV)
+    rc, ra, meta = rasterization(e3, None, None, torch.zeros(0, device=DEV),
+                                 torch.zeros(0, device=DEV), e3, cam.viewmat[None].to(DEV),
+                                 cam.K[None].to(DEV), W, H, tile_size=TS, backgrounds=bg,
+                                 covars=torch.zeros(0, 3, 3, device=DEV))
+    assert torch.equal(rc[0], bg[0].expand(H, W, 3)) and not ra.any()
+    assert meta["flatten_ids"].numel() == 0

@@ -178,3 +178,13 @@ def test_view_drop_in():
     assert tab.total_count_number == 5000 and 0 < tab.rendered_count_number <= 5000
     img2 = view(model, cam, tab)
     assert np.array_equal(img, img2)
+
+
+def test_empty_scene_frame():
+    p = {k: v[:0] for k, v in scene(10, 6).items()}
+    c2w, K = camera(1)
+    fr = FrameRenderer(dim=6, table=torch.zeros(256, 3))
+    img = fr.render(p, c2w, K, W, H, ViewState(backgrounds=(51, 102, 153)), copy=True)
+    want = np.array([51, 102, 153], np.float32) / np.float32(255.0)
+    assert np.array_equal(img, np.broadcast_to(want, img.shape))
+    assert fr.rendered_count == 0 and fr.total_count == 0

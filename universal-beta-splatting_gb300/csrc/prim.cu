@@ -638,7 +638,7 @@ static int proj_common(ProjArgs &a, int32_t C, int64_t N, const float *means,
                        const float *scales, const float *viewmats, const float *Ks, int32_t W,
                        int32_t H) {
     UBS_REQUIRE(C >= 1 && N >= 0 && W >= 0 && H >= 0, "projection: bad sizes");
-    UBS_REQUIRE(covars ? (layout == 6 || layout == 9) : (quats && scales),
+    UBS_REQUIRE(N == 0 || (covars ? (layout == 6 || layout == 9) : (quats && scales)),
                 "projection: need covars (layout 6 or 9) or quats + scales");
     a.C = C;
     a.N = N;

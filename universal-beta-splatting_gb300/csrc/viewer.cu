@@ -271,10 +271,9 @@ size_t ubs_quantile_mask_workspace_bytes(void) { return qws_bytes(); }
 int ubs_quantile_mask(int64_t n, int32_t n_arrays, const float *const *arrays,
                       const int64_t *strides, const double *quantiles, uint8_t *mask,
                       void *workspace, size_t workspace_bytes, void *stream) {
-    UBS_REQUIRE(n >= 0 && n_arrays >= 1 && n_arrays <= QM_MAX_ARR && arrays && strides &&
-                    quantiles && mask,
-                "quantile_mask: bad arguments");
+    UBS_REQUIRE(n >= 0 && n_arrays >= 1 && n_arrays <= QM_MAX_ARR, "quantile_mask: bad sizes");
     if (n == 0) return UBS_OK;
+    UBS_REQUIRE(arrays && strides && quantiles && mask, "quantile_mask: null pointer");
     UBS_REQUIRE(workspace && workspace_bytes >= qws_bytes(), "quantile_mask: workspace too small");
     QArrays va{};
     for (int a = 0; a < QM_MAX_ARR; ++a) {
