@@ -83,6 +83,10 @@ def parse():
                     help="with --profile: launch the step kernel by kernel instead of a graph")
     ap.add_argument("--dropin", action="store_true",
                     help="with --profile: the step through the drop-in gsplat operators")
+    ap.add_argument("--profile-neighbours", action="store_true",
+                    help="run each training-step neighbour (Adam, the losses, MCMC, scene "
+                         "file, viewer frame) once on the 1M scene for an ncu capture; prints "
+                         "no JSON line")
     return ap.parse_args()
 
 
@@ -599,6 +603,56 @@ def bench_viewer(p, cam, dev, reps=10):
                    "host float32 array: ubs.viewer vs the reference's view() steps on the "
                    "drop-in operators; median wall clock of %d frames" % reps)
     return res
+
+
+def profile_neighbours(p, cam, dev):
+    """One run of each training-step neighbour on the headline scene, for
+    ncu: Adam over the seven groups, the L1 + SSIM loss and the L1 loss on a
+    1920x1080 image, MCMC relocation / addition / noise, a scene-file save
+    and load, and viewer frames (RGB and Depth with quantile masks)."""
+    import tempfile
+    import types
+    from ubs import mcmc, ply
+    from ubs.loss import l1_loss as _l1, l1_ssim_loss
+    from ubs.optim import FusedAdam
+    from ubs.viewer import FrameRenderer, ViewState
+    names = ("xyz", "mean", "rgb", "opacity", "beta", "scale", "l_triangle")
+    g = torch.Generator(device="cpu").manual_seed(0)
+    m = types.SimpleNamespace()
+    for k in names:
+        t = p[k].detach().clone().reshape(p[k].shape[0], -1)
+        if k == "opacity":
+            t[torch.rand(t.shape[0], generator=g).to(dev) < 0.1] = -8.0
+        setattr(m, "_" + k, torch.nn.Parameter(t))
+    m.optimizer = FusedAdam([{"params": [getattr(m, "_" + k)], "lr": TRAIN_LRS[k], "name": k}
+                             for k in names], lr=0.0, eps=1e-15)
+    for _ in range(2):
+        for k in names:
+            prm = getattr(m, "_" + k)
+            prm.grad = torch.randn(prm.shape, device=dev) * 1e-3
+        m.optimizer.step()
+    gt = torch.rand(1, HEIGHT, WIDTH, 3, generator=g).to(dev)
+    img = (gt + 0.05 * torch.randn(gt.shape, generator=g).to(dev)).clamp(0, 1).requires_grad_(True)
+    l1_ssim_loss(img, gt, LAMBDA_DSSIM, channels_last=True).backward()
+    img.grad = None
+    _l1(img, gt).backward()
+    mcmc.relocate_gs(m)
+    mcmc.add_new_gs(m, 10 ** 9)
+    mcmc.perturb_xyz(m, 1.6e-4)
+    path = os.path.join(tempfile.gettempdir(), "ubs_profile_scene_%d.ply" % os.getpid())
+    try:
+        ply.save_ply(path, p)
+        ply.load_ply(path, dev)
+    finally:
+        if os.path.exists(path):
+            os.remove(path)
+    fr = FrameRenderer(dim=DIM, table=torch.rand(256, 3, generator=g).to(dev))
+    c2w = torch.inverse(cam.viewmat.cpu()).numpy()
+    for mode in ("RGB", "Depth"):
+        fr.render(p, c2w, cam.K.cpu().numpy(), WIDTH, HEIGHT,
+                  ViewState(b_xyz=(5, 95), b_view=(5, 95), render_mode=mode))
+    torch.cuda.synchronize()
+    print("profile run (training-step neighbours)", flush=True)
 
 
 def time_steps(fn, K, dev, flush, after=None):
@@ -1139,6 +1193,9 @@ def main():
     L.lib()
     p, cam, ri, rj, bg, target = make_problem(args.n_prims, rank, dev)
     fz = FusedStep(p, cam, bg, target, dev)
+    if args.profile_neighbours:
+        profile_neighbours(p, cam, dev)
+        return
     if args.profile and args.dropin:
         for _ in range(args.warmup + 1):
             gpu_step(p, cam, ri, rj, bg, target)

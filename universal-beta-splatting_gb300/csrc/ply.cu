@@ -21,26 +21,65 @@ namespace {
 
 struct PlyMap {
     int32_t A, n_tensors;
+    int32_t unmapped; // some record property is filled by no tensor (packed as 0)
     int32_t w[UBS_PLY_MAX_TENSORS];
+    int32_t off[UBS_PLY_MAX_TENSORS]; // first entry of each tensor in src_of
     float *p[UBS_PLY_MAX_TENSORS];
     int16_t tensor_of[UBS_PLY_MAX_PROPS];
     int16_t column_of[UBS_PLY_MAX_PROPS];
+    int16_t src_of[UBS_PLY_MAX_PROPS];  // record column of each tensor column (-1: none)
 };
 
-// One thread per record float (coalesced over the records).
+constexpr int PLY_ROWS = 32; // records per warp step
+
+// One warp per PLY_ROWS consecutive records: the records (contiguous) pass
+// through shared memory, and each tensor's PLY_ROWS rows (contiguous in the
+// tensor) are written -- or read, to pack -- as one run, so every global
+// access is coalesced and no per-element division by the record width runs
+// on 64-bit indices.
 template <bool PACK>
 __global__ void __launch_bounds__(256) ply_kernel(PlyMap m, float *records, int64_t n) {
-    const int64_t total = n * m.A;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += stride) {
-        const int64_t row = e / m.A;
-        const int c = (int)(e - row * m.A);
-        const int k = m.tensor_of[c];
-        if (PACK) {
-            records[e] = k >= 0 ? m.p[k][row * m.w[k] + m.column_of[c]] : 0.f;
-        } else if (k >= 0) {
-            m.p[k][row * m.w[k] + m.column_of[c]] = records[e];
+    extern __shared__ float sbuf[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    float *sw = sbuf + (size_t)warp * PLY_ROWS * m.A;
+    const int64_t groups = (n + PLY_ROWS - 1) / PLY_ROWS;
+    for (int64_t gi = (int64_t)blockIdx.x * wpb + warp; gi < groups; gi += (int64_t)gridDim.x * wpb) {
+        const int64_t r0 = gi * PLY_ROWS;
+        const int rows = (int)(n - r0 < PLY_ROWS ? n - r0 : PLY_ROWS);
+        const int cnt = rows * m.A;
+        float *rec = records + r0 * m.A;
+        if (!PACK) {
+            for (int e = lane; e < cnt; e += 32) sw[e] = rec[e];
+            __syncwarp();
+            for (int k = 0; k < m.n_tensors; ++k) {
+                const int w = m.w[k];
+                float *dst = m.p[k] + r0 * w;
+                for (int e = lane; e < rows * w; e += 32) {
+                    const int r = e / w, c = e - r * w;
+                    const int s = m.src_of[m.off[k] + c];
+                    if (s >= 0) dst[e] = sw[r * m.A + s];
+                }
+            }
+        } else {
+            if (m.unmapped)
+                for (int e = lane; e < cnt; e += 32) {
+                    const int r = e / m.A, c = e - r * m.A;
+                    if (m.tensor_of[c] < 0) sw[e] = 0.f; // properties no tensor fills
+                }
+            for (int k = 0; k < m.n_tensors; ++k) {
+                const int w = m.w[k];
+                const float *src = m.p[k] + r0 * w;
+                for (int e = lane; e < rows * w; e += 32) {
+                    const int r = e / w, c = e - r * w;
+                    const int s = m.src_of[m.off[k] + c];
+                    if (s >= 0) sw[r * m.A + s] = src[e];
+                }
+            }
+            __syncwarp();
+            for (int e = lane; e < cnt; e += 32) rec[e] = sw[e];
         }
+        __syncwarp();
     }
 }
 
@@ -56,14 +95,26 @@ int load_map(const ubs_ply_layout *l, PlyMap &m) {
         m.p[k] = k < l->n_tensors ? l->param[k] : nullptr;
         if (k < l->n_tensors) UBS_REQUIRE(m.p[k] && m.w[k] >= 1, "ply: bad tensor %d", k);
     }
+    int total = 0;
+    for (int k = 0; k < UBS_PLY_MAX_TENSORS; ++k) {
+        m.off[k] = total;
+        total += m.w[k];
+    }
+    UBS_REQUIRE(total <= UBS_PLY_MAX_PROPS, "ply: more than %d tensor columns", UBS_PLY_MAX_PROPS);
+    for (int i = 0; i < UBS_PLY_MAX_PROPS; ++i) m.src_of[i] = -1;
+    m.unmapped = 0;
     for (int c = 0; c < UBS_PLY_MAX_PROPS; ++c) {
         const bool in = c < m.A;
         m.tensor_of[c] = in ? l->tensor_of[c] : -1;
         m.column_of[c] = in ? l->column_of[c] : 0;
-        if (in && m.tensor_of[c] >= 0)
+        if (in && m.tensor_of[c] >= 0) {
             UBS_REQUIRE(m.tensor_of[c] < m.n_tensors && m.column_of[c] >= 0 &&
                             m.column_of[c] < m.w[m.tensor_of[c]],
                         "ply: property %d maps outside its tensor", c);
+            m.src_of[m.off[m.tensor_of[c]] + m.column_of[c]] = (int16_t)c;
+        } else if (in) {
+            m.unmapped = 1;
+        }
     }
     return UBS_OK;
 }
@@ -219,13 +270,19 @@ static int ply_launch(const ubs_ply_layout *layout, float *records, int64_t n, v
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t want = (n * m.A + 255) / 256;
+    // warps per block by the shared memory one warp's records take (<= 48 KB)
+    const size_t per_warp = (size_t)PLY_ROWS * m.A * sizeof(float);
+    int wpb = (int)((48 * 1024) / per_warp);
+    wpb = wpb < 1 ? 1 : (wpb > 8 ? 8 : wpb);
+    const int64_t groups = (n + PLY_ROWS - 1) / PLY_ROWS;
+    const int64_t want = (groups + wpb - 1) / wpb;
     const unsigned grid = (unsigned)(want < (int64_t)sms * 16 ? want : (int64_t)sms * 16);
+    const size_t smem = per_warp * wpb;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (pack)
-        UBS_TIMED("ply_pack", st, ply_kernel<true><<<grid, 256, 0, st>>>(m, records, n));
+        UBS_TIMED("ply_pack", st, ply_kernel<true><<<grid, 32 * wpb, smem, st>>>(m, records, n));
     else
-        UBS_TIMED("ply_unpack", st, ply_kernel<false><<<grid, 256, 0, st>>>(m, records, n));
+        UBS_TIMED("ply_unpack", st, ply_kernel<false><<<grid, 32 * wpb, smem, st>>>(m, records, n));
     note_launch();
     return check_launch(pack ? "ply_pack" : "ply_unpack");
 }
