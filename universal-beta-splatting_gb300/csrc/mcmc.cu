@@ -22,6 +22,7 @@
 // The random stream differs from torch.multinomial's; given the same draws
 // (the given_src arguments) the results are the reference's.
 #include <cfloat>
+#include <cstdint>
 
 #include "ubs_common.cuh"
 
@@ -373,9 +374,18 @@ __global__ void __launch_bounds__(MC_THREADS) grow_kernel(McmcSet old, McmcSet g
     const int wd = old.w[k];
     const int64_t total = (n + n_add) * wd;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const bool small = total < INT32_MAX; // 32-bit row / column split (the usual case)
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += stride) {
-        const int64_t row = e / wd;
-        const int col = (int)(e - row * wd);
+        int64_t row;
+        int col;
+        if (small) {
+            const uint32_t e32 = (uint32_t)e, r32 = e32 / (uint32_t)wd;
+            row = r32;
+            col = (int)(e32 - r32 * (uint32_t)wd);
+        } else {
+            row = e / wd;
+            col = (int)(e - row * wd);
+        }
         float val;
         if (row < n) {
             const int c = w.count[row];
