@@ -251,7 +251,7 @@ int ubs_adam_step(int32_t n_tensors, const void *device_table, const float *devi
 /* ----------------------------------------------------------------- loss ---
  * The training loss  weight_l1 * mean|img - gt| + weight_ssim * mean(SSIM map)
  * + weight_const  over a batch of images, with its gradient w.r.t. img in the
- * same launch.  SSIM as utils/loss_utils.py:26-80 defines it (11 x 11 Gaussian
+ * same call.  SSIM as utils/loss_utils.py:26-80 defines it (11 x 11 Gaussian
  * window, sigma 1.5, zero padding, C1 = 0.01^2, C2 = 0.03^2) and as the
  * fused_ssim package evaluates it for train.py:117-121; valid_padding != 0
  * averages the map only over points at least 5 pixels from every edge

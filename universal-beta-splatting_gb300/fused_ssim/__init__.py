@@ -4,8 +4,9 @@
 fused_ssim(img1, img2, padding="same", train=True) returns the mean SSIM of
 img1 [N, C, H, W] against img2 as a 0-dim tensor, differentiable w.r.t. img1
 (img2 is the target), with SSIM as utils/loss_utils.py:26-80 defines it.  The
-whole computation, gradient included, is one launch of the library's loss
-kernel (ubs.loss); train=False skips the gradient.
+whole computation, gradient included, is one call of the library's loss
+(ubs.loss: a statistics kernel and a gradient kernel); train=False skips the
+gradient kernel.
 """
 import torch
 

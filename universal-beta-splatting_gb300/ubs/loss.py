@@ -1,4 +1,4 @@
-"""The reference's training loss in one kernel launch (csrc/ssim.cu).
+"""The reference's training loss in two kernel launches (csrc/ssim.cu).
 
 train.py:117-121 trains on  (1 - l) L1(image, gt) + l (1 - SSIM(image, gt))
 (l = lambda_dssim, 0.2) with SSIM from the fused_ssim package, which
