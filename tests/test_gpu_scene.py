@@ -95,6 +95,31 @@ def test_fused_multiview_mixed_resolution():
         assert rel_l2(leaves_f[k].grad, grads[k]) < 1e-4, (k, rel_l2(leaves_f[k].grad, grads[k]))
 
 
+@pytest.mark.parametrize("N,D", [(50, 7), (129, 6)])
+def test_fused_multiview_few_primitives(N, D):
+    # the per-primitive kernels work in CTAs of 128 (view, primitive)
+    # entries: with N < 128 one CTA holds entries of three or more views
+    p = make_params(N, D, seed=N)
+    p["scale"][:, :3] += 1.0
+    cams = [S.orbit_view(v, 3.0, 64 + 16 * v, 48, 60.0, 60.0, timestamp=0.1 * v, device=DEV)
+            for v in range(4)]
+    bgs = torch.rand(4, 3, generator=torch.Generator().manual_seed(1)).to(DEV)
+    _, views, colors, alphas, leaves_f = fused_render(p, cams, bgs)
+    imgs = views.split(colors)
+    g = torch.Generator().manual_seed(9)
+    ws = [torch.randn(c.height, c.width, 3, generator=g).to(DEV) for c in cams]
+    sum((im * w).sum() for im, w in zip(imgs, ws)).backward()
+    grads = {k: torch.zeros_like(v) for k, v in p.items()}
+    for v, cam in enumerate(cams):
+        img_d, _, leaves_d = dropin_render(p, cam, bgs[v])
+        assert float((imgs[v] - img_d).abs().max()) < 1e-5, v
+        (img_d * ws[v]).sum().backward()
+        for k in grads:
+            grads[k] += leaves_d[k].grad
+    for k in grads:
+        assert rel_l2(leaves_f[k].grad, grads[k]) < 1e-4, (k, rel_l2(leaves_f[k].grad, grads[k]))
+
+
 def test_fused_capacity_overflow_is_recovered():
     p = make_params(4000, 6, seed=21)
     cam = S.orbit_view(7, 3.0, 256, 192, 220.0, 220.0, device=DEV)

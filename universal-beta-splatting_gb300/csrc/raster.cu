@@ -148,20 +148,21 @@ __global__ void pack_records_kernel(int64_t T, int64_t n_prims, const int32_t *_
 // ------------------------------------------------------ shared helpers
 // Thread layout: every thread owns two vertically adjacent pixels, a warp an
 // 8x8-pixel footprint; a TS x TS tile has (TS/8)^2 warps = TS*TS/2 threads and
-// streams its records in batches of TS*TS, two batch slots per thread in the
-// culling phase.
+// streams its records in batches of RB*TS*TS/2, RB batch slots per thread in
+// the culling phase (RB = 2, or 1 in the backward of tiles up to 16 x 16,
+// whose smaller footprint fits 8 CTAs per SM).
 struct SmemLayout {
     int mask_off, rec_off, col_off, gacc_off, touched_off, total;
 };
 
 template <int CD, bool PACK, bool BWD>
-__host__ __device__ inline SmemLayout smem_layout(int NT) {
+__host__ __device__ inline SmemLayout smem_layout(int NT, int RB = 2) {
     constexpr int NV = 7 + CD; // gradient values per record
-    const int nw = NT / 32, BR = 2 * NT;
+    const int nw = NT / 32, BR = RB * NT;
     SmemLayout L;
     L.mask_off = 16; // after two mbarriers
-    // per-target-warp masks (nw x 2nw words), then one int per warp
-    L.rec_off = (L.mask_off + nw * 2 * nw * 4 + nw * 4 + 127) & ~127;
+    // per-target-warp masks (nw x RB nw words), then one int per warp
+    L.rec_off = (L.mask_off + nw * RB * nw * 4 + nw * 4 + 127) & ~127;
     const int colbytes = PACK ? 16 : CD * 4;
     L.col_off = L.rec_off + 2 * BR * (int)sizeof(GeoRec);
     L.gacc_off = (L.col_off + 2 * BR * colbytes + 15) & ~15;
@@ -218,15 +219,17 @@ __device__ __forceinline__ void issue_batch(const RasterArgs &a, GeoRec *srec, f
     if (PACK) bulk_g2s(scol4 + buf * BR, a.rcols + bs, (uint32_t)cnt * 16u, &mbar[buf]);
 }
 
-// Per-batch culling masks.  Thread tid describes batch slots tid and tid + NT;
-// for every warp w one ballot per slot gives 32 bits of w's 2*nw-word mask
-// (word k covers slots 32k .. 32k+31, so ascending bits are front to back).
-// limit[w] (backward) drops records past warp w's last contributor.
+// Per-batch culling masks.  Thread tid describes batch slots tid + h NT
+// (h < RB); for every warp w one ballot per slot gives 32 bits of w's
+// RB*nw-word mask (word k covers slots 32k .. 32k+31, so ascending bits are
+// front to back).  limit[w] (backward) drops records past warp w's last
+// contributor.
+template <int RB = 2>
 __device__ __forceinline__ void build_masks(const GeoRec *batch, int cnt, int lo, int NT, int nw,
                                             int wpr, int tile_x0, int tile_y0, int tid, int lane,
                                             uint32_t *wmask, const int32_t *limit) {
 #pragma unroll
-    for (int half = 0; half < 2; ++half) {
+    for (int half = 0; half < RB; ++half) {
         const int s = tid + half * NT;
         const bool valid = s < cnt;
         GeoRec r;
@@ -242,7 +245,7 @@ __device__ __forceinline__ void build_masks(const GeoRec *batch, int cnt, int lo
             bool ov = valid && ellipse_hits_box(r, pd, x0, y0);
             if (limit) ov = ov && (lo + s <= limit[w]);
             const uint32_t bits = __ballot_sync(0xffffffffu, ov);
-            if (lane == 0) wmask[w * 2 * nw + word] = bits;
+            if (lane == 0) wmask[w * RB * nw + word] = bits;
         }
     }
 }
@@ -613,15 +616,18 @@ template <int OFF> struct ReduceChunks<OFF, 0> {
     static __device__ __forceinline__ void run(const float (&)[NV], int, float *) {}
 };
 
-template <int CD, bool PACK>
-__global__ void __launch_bounds__(512) raster_bwd_kernel(RasterArgs a) {
+// RB = 1 serves tiles of at most 128 threads at 8 CTAs per SM (64 registers,
+// about 18 KB of shared memory); RB = 2 the larger tiles.
+template <int CD, bool PACK, int RB>
+__global__ void __launch_bounds__(RB == 1 ? 128 : 512, RB == 1 ? 8 : 1)
+    raster_bwd_kernel(RasterArgs a) {
     constexpr int NV = 7 + CD;
     extern __shared__ __align__(128) unsigned char sm[];
-    const int NT = blockDim.x, nw = NT >> 5, BR = 2 * NT;
-    const SmemLayout L = smem_layout<CD, PACK, true>(NT);
+    const int NT = blockDim.x, nw = NT >> 5, BR = RB * NT;
+    const SmemLayout L = smem_layout<CD, PACK, true>(NT, RB);
     uint64_t *mbar = reinterpret_cast<uint64_t *>(sm);
     uint32_t *wmask = reinterpret_cast<uint32_t *>(sm + L.mask_off);
-    int32_t *wbin = reinterpret_cast<int32_t *>(sm + L.mask_off + nw * 2 * nw * 4);
+    int32_t *wbin = reinterpret_cast<int32_t *>(sm + L.mask_off + nw * RB * nw * 4);
     GeoRec *srec = reinterpret_cast<GeoRec *>(sm + L.rec_off);
     float4 *scol4 = reinterpret_cast<float4 *>(sm + L.col_off);
     float *scol = reinterpret_cast<float *>(sm + L.col_off);
@@ -693,22 +699,24 @@ __global__ void __launch_bounds__(512) raster_bwd_kernel(RasterArgs a) {
         if (tid == 0 && ok) waited = b + 1;
         const GeoRec *batch = srec + buf * BR;
         const int32_t gid0 = (tid < cnt) ? batch[tid].gid : 0;
-        const int32_t gid1 = (tid + NT < cnt) ? batch[tid + NT].gid : 0;
+        const int32_t gid1 = (RB > 1 && tid + NT < cnt) ? batch[tid + NT].gid : 0;
         // per-slot opacity and beta for the flush (the buffer may be refilled
         // while other threads still flush)
         const float op0 = (tid < cnt) ? batch[tid].opac : 0.f;
         const float be0 = (tid < cnt) ? batch[tid].beta : 0.f;
-        const float op1 = (tid + NT < cnt) ? batch[tid + NT].opac : 0.f;
-        const float be1 = (tid + NT < cnt) ? batch[tid + NT].beta : 0.f;
+        const float op1 = (RB > 1 && tid + NT < cnt) ? batch[tid + NT].opac : 0.f;
+        const float be1 = (RB > 1 && tid + NT < cnt) ? batch[tid + NT].beta : 0.f;
         const float3 cn0 = (tid < cnt) ? make_float3(batch[tid].cxx, batch[tid].cxy, batch[tid].cyy)
                                        : make_float3(0.f, 0.f, 0.f);
-        const float3 cn1 = (tid + NT < cnt) ? make_float3(batch[tid + NT].cxx, batch[tid + NT].cxy,
-                                                          batch[tid + NT].cyy)
-                                            : make_float3(0.f, 0.f, 0.f);
-        build_masks(batch, cnt, lo, NT, nw, wpr, tx * a.TS, ty * a.TS, tid, lane, wmask, wbin);
+        const float3 cn1 = (RB > 1 && tid + NT < cnt)
+                               ? make_float3(batch[tid + NT].cxx, batch[tid + NT].cxy,
+                                             batch[tid + NT].cyy)
+                               : make_float3(0.f, 0.f, 0.f);
+        build_masks<RB>(batch, cnt, lo, NT, nw, wpr, tx * a.TS, ty * a.TS, tid, lane, wmask,
+                        wbin);
         if (!PACK) {
 #pragma unroll
-            for (int half = 0; half < 2; ++half) {
+            for (int half = 0; half < RB; ++half) {
                 const int sl = tid + half * NT;
                 if (sl < cnt) {
                     const float *cp = a.colors + (int64_t)(half ? gid1 : gid0) * CD;
@@ -721,8 +729,8 @@ __global__ void __launch_bounds__(512) raster_bwd_kernel(RasterArgs a) {
             if (tid == 0) atomicOr(a.status, DEV_ERR_WAIT_TIMEOUT);
             break;
         }
-        for (int k = 2 * nw - 1; k >= 0; --k) {
-            uint32_t m = wmask[warp * 2 * nw + k];
+        for (int k = RB * nw - 1; k >= 0; --k) {
+            uint32_t m = wmask[warp * RB * nw + k];
             while (m) {
                 const int bit = 31 - __clz(m);
                 m &= ~(1u << bit);
@@ -739,7 +747,7 @@ __global__ void __launch_bounds__(512) raster_bwd_kernel(RasterArgs a) {
         }
         __syncthreads();
 #pragma unroll
-        for (int half = 0; half < 2; ++half) {
+        for (int half = 0; half < RB; ++half) {
             const int sl = tid + half * NT;
             if (sl < cnt && touched[sl]) {
                 const int64_t gg = half ? gid1 : gid0;
@@ -809,13 +817,14 @@ template <int CD, bool BWD>
 static int launch_blend(RasterArgs &a, cudaStream_t st) {
     constexpr bool PACK = CD <= 4;
     const int NT = a.TS * a.TS / 2; // two pixels per thread
-    const SmemLayout L = smem_layout<CD, PACK, BWD>(NT);
+    const int RB = (BWD && NT <= 128) ? 1 : 2;
+    const SmemLayout L = smem_layout<CD, PACK, BWD>(NT, RB);
     if (L.total > 227 * 1024)
         return set_error(UBS_ERR_UNSUPPORTED, "raster: tile_size %d with %d channels needs %d B "
                                               "of shared memory", a.TS, CD, L.total);
     const unsigned nblocks = (unsigned)a.n_buckets;
     if (nblocks == 0) return UBS_OK;
-    auto k = BWD ? raster_bwd_kernel<CD, PACK>
+    auto k = BWD ? (RB == 1 ? raster_bwd_kernel<CD, PACK, 1> : raster_bwd_kernel<CD, PACK, 2>)
                  : (a.pair_count ? raster_fwd_kernel<CD, PACK, true>
                                  : raster_fwd_kernel<CD, PACK, false>);
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total) !=
