@@ -149,8 +149,9 @@ __global__ void pack_records_kernel(int64_t T, int64_t n_prims, const int32_t *_
 // Thread layout: every thread owns two vertically adjacent pixels, a warp an
 // 8x8-pixel footprint; a TS x TS tile has (TS/8)^2 warps = TS*TS/2 threads and
 // streams its records in batches of RB*TS*TS/2, RB batch slots per thread in
-// the culling phase (RB = 2, or 1 in the backward of tiles up to 16 x 16,
-// whose smaller footprint fits 8 CTAs per SM).
+// the culling phase (RB = 1 in the backward of tiles up to 16 x 16 with packed
+// colours of at most 4 channels, whose smaller shared footprint lets 8 CTAs
+// share an SM; else 2).
 struct SmemLayout {
     int mask_off, rec_off, col_off, gacc_off, touched_off, total;
 };
@@ -320,11 +321,12 @@ __device__ __forceinline__ void blend_pair(const GeoRec &q, const float (&col)[C
 }
 
 // --------------------------------------------------------------- forward
-template <int CD, bool PACK, bool COUNT>
-__global__ void __launch_bounds__(512) raster_fwd_kernel(RasterArgs a) {
+// MINB > 1: tiles of at most 128 threads, MINB CTAs per SM.
+template <int CD, bool PACK, bool COUNT, int RB, int MINB>
+__global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_fwd_kernel(RasterArgs a) {
     extern __shared__ __align__(128) unsigned char sm[];
-    const int NT = blockDim.x, nw = NT >> 5, BR = 2 * NT;
-    const SmemLayout L = smem_layout<CD, PACK, false>(NT);
+    const int NT = blockDim.x, nw = NT >> 5, BR = RB * NT;
+    const SmemLayout L = smem_layout<CD, PACK, false>(NT, RB);
     uint64_t *mbar = reinterpret_cast<uint64_t *>(sm);
     uint32_t *wmask = reinterpret_cast<uint32_t *>(sm + L.mask_off);
     GeoRec *srec = reinterpret_cast<GeoRec *>(sm + L.rec_off);
@@ -398,11 +400,11 @@ __global__ void __launch_bounds__(512) raster_fwd_kernel(RasterArgs a) {
             const bool ok = mbar_wait_bounded(&mbar[buf], (b >> 1) & 1);
             if (tid == 0 && ok) waited = b + 1;
             const GeoRec *batch = srec + buf * BR;
-            build_masks(batch, cnt, 0, NT, nw, wpr, tx * a.TS, ty * a.TS, tid, lane, wmask,
-                        nullptr);
+            build_masks<RB>(batch, cnt, 0, NT, nw, wpr, tx * a.TS, ty * a.TS, tid, lane, wmask,
+                            nullptr);
             if (!PACK) {
 #pragma unroll
-                for (int half = 0; half < 2; ++half) {
+                for (int half = 0; half < RB; ++half) {
                     const int s = tid + half * NT;
                     if (s < cnt) {
                         const float *cp = a.colors + (int64_t)batch[s].gid * CD;
@@ -418,8 +420,8 @@ __global__ void __launch_bounds__(512) raster_fwd_kernel(RasterArgs a) {
             }
             if (!__all_sync(0xffffffffu, d0 && d1)) {
                 bool warp_done = false;
-                for (int k = 0; k < 2 * nw && !warp_done; ++k) {
-                    uint32_t m = wmask[warp * 2 * nw + k];
+                for (int k = 0; k < RB * nw && !warp_done; ++k) {
+                    uint32_t m = wmask[warp * RB * nw + k];
                     while (m) {
                         const int bit = __ffs(m) - 1;
                         m &= m - 1;
@@ -616,11 +618,9 @@ template <int OFF> struct ReduceChunks<OFF, 0> {
     static __device__ __forceinline__ void run(const float (&)[NV], int, float *) {}
 };
 
-// RB = 1 serves tiles of at most 128 threads at 8 CTAs per SM (64 registers,
-// about 18 KB of shared memory); RB = 2 the larger tiles.
-template <int CD, bool PACK, int RB>
-__global__ void __launch_bounds__(RB == 1 ? 128 : 512, RB == 1 ? 8 : 1)
-    raster_bwd_kernel(RasterArgs a) {
+// MINB > 1: tiles of at most 128 threads, MINB CTAs per SM.
+template <int CD, bool PACK, int RB, int MINB>
+__global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_bwd_kernel(RasterArgs a) {
     constexpr int NV = 7 + CD;
     extern __shared__ __align__(128) unsigned char sm[];
     const int NT = blockDim.x, nw = NT >> 5, BR = RB * NT;
@@ -817,16 +817,28 @@ template <int CD, bool BWD>
 static int launch_blend(RasterArgs &a, cudaStream_t st) {
     constexpr bool PACK = CD <= 4;
     const int NT = a.TS * a.TS / 2; // two pixels per thread
-    const int RB = (BWD && NT <= 128) ? 1 : 2;
+    // Tiles of at most 128 threads with packed colours run 8 CTAs per SM (7
+    // for the backward of 4 channels; wider colour rows need more registers),
+    // the backward in batches of NT records to fit its shared memory.
+    const bool small = PACK && NT <= 128;
+    const int RB = (small && BWD) ? 1 : 2;
     const SmemLayout L = smem_layout<CD, PACK, BWD>(NT, RB);
     if (L.total > 227 * 1024)
         return set_error(UBS_ERR_UNSUPPORTED, "raster: tile_size %d with %d channels needs %d B "
                                               "of shared memory", a.TS, CD, L.total);
     const unsigned nblocks = (unsigned)a.n_buckets;
     if (nblocks == 0) return UBS_OK;
-    auto k = BWD ? (RB == 1 ? raster_bwd_kernel<CD, PACK, 1> : raster_bwd_kernel<CD, PACK, 2>)
-                 : (a.pair_count ? raster_fwd_kernel<CD, PACK, true>
-                                 : raster_fwd_kernel<CD, PACK, false>);
+    void (*k)(RasterArgs) = nullptr;
+    if constexpr (PACK) {
+        if (small)
+            k = BWD ? raster_bwd_kernel<CD, PACK, 1, (CD < 4 ? 8 : 7)>
+                    : (a.pair_count ? raster_fwd_kernel<CD, PACK, true, 2, 8>
+                                    : raster_fwd_kernel<CD, PACK, false, 2, 8>);
+    }
+    if (!k)
+        k = BWD ? raster_bwd_kernel<CD, PACK, 2, 1>
+                : (a.pair_count ? raster_fwd_kernel<CD, PACK, true, 2, 1>
+                                : raster_fwd_kernel<CD, PACK, false, 2, 1>);
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total) !=
         cudaSuccess)
         return check_launch("raster smem attribute");
