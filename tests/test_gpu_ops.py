@@ -234,6 +234,8 @@ def _blend_inputs(N, W, H, C, seed, ts, channels=3, big_frac=0.0):
     (1, 4000, 256, 192, 16, 3, False),
     (1, 4000, 256, 192, 16, 3, True),
     (2, 3000, 200, 150, 16, 4, True),
+    (1, 2500, 160, 120, 16, 2, True),
+    (1, 2500, 160, 120, 16, 1, False),
     (1, 2500, 160, 120, 8, 1, False),
     (1, 2500, 160, 120, 32, 3, True),
     (1, 2000, 128, 96, 16, 8, True),
