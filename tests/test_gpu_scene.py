@@ -120,6 +120,21 @@ def test_fused_multiview_few_primitives(N, D):
         assert rel_l2(leaves_f[k].grad, grads[k]) < 1e-4, (k, rel_l2(leaves_f[k].grad, grads[k]))
 
 
+def test_fused_many_tiles_match_dropin():
+    # 3 views of 1920x1080 at 16x16 tiles: 24,480 (view, tile) buckets, so
+    # the single-CTA launch-order pass walks its buckets in many strides
+    p = make_params(3000, 6, seed=31)
+    cams = [S.orbit_view(40 + v, 3.0, 1920, 1080, 1500.0, 1500.0, device=DEV) for v in range(3)]
+    bgs = torch.rand(3, 3, generator=torch.Generator().manual_seed(2)).to(DEV)
+    _, views, colors, alphas, _ = fused_render(p, cams, bgs)
+    assert views.n_buckets > 16384
+    imgs = views.split(colors)
+    for v, cam in enumerate(cams):
+        img_d, _, _ = dropin_render(p, cam, bgs[v])
+        assert float((imgs[v] - img_d).detach().abs().max()) < 1e-5, v
+    assert float(alphas.max()) > 0.5
+
+
 def test_fused_capacity_overflow_is_recovered():
     p = make_params(4000, 6, seed=21)
     cam = S.orbit_view(7, 3.0, 256, 192, 220.0, 220.0, device=DEV)
