@@ -65,6 +65,13 @@ struct RasterArgs {
     int32_t n_buckets;          // total (view, tile) buckets
     const int64_t *n_isects_dev; // device-side intersection count (nullptr: n_isects)
     const int32_t *order;        // CTA -> bucket launch order (nullptr: identity)
+    // gather mode (fused scene path, packed colours): records are copied per
+    // batch from the per-entry tables, addressed by the low word of the
+    // sorted (depth, entry) keys, instead of from sorted copies
+    const uint64_t *keys;       // nullptr: sorted copies in recs / rcols
+    const GeoRec *entry_recs;   // [C*N] one record per (view, primitive) entry
+    const float4 *prim_cols;    // [N] packed colour per primitive
+    int64_t n_per_view;         // N
 };
 
 // Where a (view, tile) bucket lives: view, tile within the view, image size,
@@ -206,6 +213,54 @@ __device__ __forceinline__ bool ellipse_hits_box(const GeoRec &r, bool pd, float
         best = fminf(best, r.cxx * dx * dx + 2.f * r.cxy * dx * dy + r.cyy * dy * dy);
     }
     return best < 1.01f;
+}
+
+// Gather mode: thread tid copies batch slots tid + h NT (h < RB) with
+// cp.async and arrives on the batch's mbarrier once its copies have landed;
+// the mbarrier expects one arrival per thread.  Entry indices are loaded one
+// batch ahead of their copies (load_entries) so the copies never wait on the
+// key reads.  The keys of a bucket address entries of the bucket's view,
+// [lo_e, hi_e]; indices are clamped to that range.
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_arrive(uint64_t *bar) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+template <int RB>
+__device__ __forceinline__ void load_entries(const RasterArgs &a, int32_t bs, int cnt, int NT,
+                                             int tid, int32_t (&ent)[RB]) {
+#pragma unroll
+    for (int h = 0; h < RB; ++h) {
+        const int s = tid + h * NT;
+        ent[h] = s < cnt ? (int32_t)(uint32_t)a.keys[bs + s] : 0;
+    }
+}
+
+template <int RB>
+__device__ __forceinline__ void gather_batch(const RasterArgs &a, GeoRec *srec, float4 *scol4,
+                                             uint64_t *mbar, int BR, int buf, int cnt,
+                                             const int32_t (&ent)[RB], int64_t lo_e,
+                                             int64_t hi_e, int NT, int tid) {
+#pragma unroll
+    for (int h = 0; h < RB; ++h) {
+        const int s = tid + h * NT;
+        if (s < cnt) {
+            const int64_t e = min(max((int64_t)ent[h], lo_e), hi_e);
+            const char *src = reinterpret_cast<const char *>(a.entry_recs + e);
+            char *dst = reinterpret_cast<char *>(srec + buf * BR + s);
+            cp_async16(dst, src);
+            cp_async16(dst + 16, src + 16);
+            cp_async16(scol4 + buf * BR + s, a.prim_cols + (e - lo_e));
+        }
+    }
+    cp_async_arrive(&mbar[buf]);
 }
 
 // Issues the bulk copies of batch [bs, bs+cnt) into buffer `buf` (thread 0).
@@ -377,14 +432,24 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_fwd_kernel(
     bool d0 = !in0, d1 = !in1;
 
     if (nb > 0) {
+        const bool gather = PACK && a.keys != nullptr;
+        const int64_t lo_e = gather ? (int64_t)cam * a.n_per_view : 0;
+        const int64_t hi_e = lo_e + a.n_per_view - 1;
+        int32_t ent[RB];
         if (tid == 0) {
-            mbar_init(&mbar[0], 1);
-            mbar_init(&mbar[1], 1);
+            mbar_init(&mbar[0], gather ? NT : 1);
+            mbar_init(&mbar[1], gather ? NT : 1);
             fence_barrier_init();
         }
         __syncthreads();
         int issued = 0, waited = 0;
-        if (tid == 0) {
+        if (gather) {
+            load_entries<RB>(a, rs, min(BR, re - rs), NT, tid, ent);
+            gather_batch<RB>(a, srec, scol4, mbar, BR, 0, min(BR, re - rs), ent, lo_e, hi_e, NT,
+                             tid);
+            if (nb > 1) load_entries<RB>(a, rs + BR, min(BR, re - rs - BR), NT, tid, ent);
+            issued = 1;
+        } else if (tid == 0) {
             issue_batch<PACK>(a, srec, scol4, mbar, BR, 0, rs, min(BR, re - rs));
             issued = 1;
         }
@@ -392,10 +457,18 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_fwd_kernel(
             const int32_t bs = rs + b * BR;
             const int cnt = min(BR, re - bs);
             const int buf = b & 1;
-            if (tid == 0 && b + 1 < nb) {
+            if (b + 1 < nb) {
                 const int32_t bn = bs + BR;
-                issue_batch<PACK>(a, srec, scol4, mbar, BR, buf ^ 1, bn, min(BR, re - bn));
-                issued = b + 2;
+                if (gather) {
+                    gather_batch<RB>(a, srec, scol4, mbar, BR, buf ^ 1, min(BR, re - bn), ent,
+                                     lo_e, hi_e, NT, tid);
+                    if (b + 2 < nb)
+                        load_entries<RB>(a, bn + BR, min(BR, re - bn - BR), NT, tid, ent);
+                    issued = b + 2;
+                } else if (tid == 0) {
+                    issue_batch<PACK>(a, srec, scol4, mbar, BR, buf ^ 1, bn, min(BR, re - bn));
+                    issued = b + 2;
+                }
             }
             const bool ok = mbar_wait_bounded(&mbar[buf], (b >> 1) & 1);
             if (tid == 0 && ok) waited = b + 1;
@@ -440,7 +513,8 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_fwd_kernel(
             }
             if (__syncthreads_count(d0 && d1) == NT) break;
         }
-        // no bulk copy may still target this CTA's shared memory at exit
+        // no copy may still target this CTA's shared memory at exit
+        if (gather) cp_async_wait_all();
         if (tid == 0)
             for (int b = waited; b < issued; ++b)
                 if (!mbar_wait_bounded(&mbar[b & 1], (b >> 1) & 1))
@@ -667,9 +741,12 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_bwd_kernel(
     if (lane == 0) wbin[warp] = wb;
     for (int t = tid; t < BR * NV; t += NT) gacc[t] = 0.f;
     for (int t = tid; t < BR; t += NT) touched[t] = 0;
+    const bool gather = PACK && a.keys != nullptr;
+    const int64_t lo_e = gather ? (int64_t)cam * a.n_per_view : 0;
+    const int64_t hi_e = lo_e + a.n_per_view - 1;
     if (tid == 0) {
-        mbar_init(&mbar[0], 1);
-        mbar_init(&mbar[1], 1);
+        mbar_init(&mbar[0], gather ? NT : 1);
+        mbar_init(&mbar[1], gather ? NT : 1);
         fence_barrier_init();
     }
     __syncthreads();
@@ -678,22 +755,44 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_bwd_kernel(
     const int32_t hi_end = max(rs, min(re, block_bin + 1)); // exclusive upper index
     const int nb = (hi_end - rs + BR - 1) / BR;
 
+    // batch b covers [max(rs, hi_end - (b + 1) BR), hi_end - b BR): back to front
     int issued = 0, waited = 0;
-    if (nb > 0 && tid == 0) {
+    int32_t ent[RB];
+    if (nb > 0) {
         const int32_t lo = max(rs, hi_end - BR);
-        issue_batch<PACK>(a, srec, scol4, mbar, BR, 0, lo, hi_end - lo);
-        issued = 1;
+        if (gather) {
+            load_entries<RB>(a, lo, hi_end - lo, NT, tid, ent);
+            gather_batch<RB>(a, srec, scol4, mbar, BR, 0, hi_end - lo, ent, lo_e, hi_e, NT, tid);
+            if (nb > 1) {
+                const int32_t l1 = max(rs, lo - BR);
+                load_entries<RB>(a, l1, lo - l1, NT, tid, ent);
+            }
+            issued = 1;
+        } else if (tid == 0) {
+            issue_batch<PACK>(a, srec, scol4, mbar, BR, 0, lo, hi_end - lo);
+            issued = 1;
+        }
     }
     for (int b = 0; b < nb; ++b) {
         const int32_t hi = hi_end - b * BR;
         const int32_t lo = max(rs, hi - BR);
         const int cnt = hi - lo;
         const int buf = b & 1;
-        if (tid == 0 && b + 1 < nb) {
+        if (b + 1 < nb) {
             const int32_t hn = hi - BR;
             const int32_t ln = max(rs, hn - BR);
-            issue_batch<PACK>(a, srec, scol4, mbar, BR, buf ^ 1, ln, hn - ln);
-            issued = b + 2;
+            if (gather) {
+                gather_batch<RB>(a, srec, scol4, mbar, BR, buf ^ 1, hn - ln, ent, lo_e, hi_e, NT,
+                                 tid);
+                if (b + 2 < nb) {
+                    const int32_t l2 = max(rs, ln - BR);
+                    load_entries<RB>(a, l2, ln - l2, NT, tid, ent);
+                }
+                issued = b + 2;
+            } else if (tid == 0) {
+                issue_batch<PACK>(a, srec, scol4, mbar, BR, buf ^ 1, ln, hn - ln);
+                issued = b + 2;
+            }
         }
         const bool ok = mbar_wait_bounded(&mbar[buf], (b >> 1) & 1);
         if (tid == 0 && ok) waited = b + 1;
@@ -775,6 +874,8 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_bwd_kernel(
             }
         }
     }
+    // no copy may still target this CTA's shared memory at exit
+    if (gather) cp_async_wait_all();
     if (tid == 0)
         for (int b = waited; b < issued; ++b)
             if (!mbar_wait_bounded(&mbar[b & 1], (b >> 1) & 1))
@@ -932,8 +1033,8 @@ static void fill_common(RasterArgs &a, int32_t C, int64_t N, int32_t ch, int64_t
 // with the records, per-view grids, intersection count read on the device.
 int scene_blend(int fwd, int32_t C, int64_t CN, int32_t n_buckets, int32_t tile_size,
                 const int32_t *offsets, const int32_t *order, const int64_t *T_dev, int64_t cap,
-                const void *recs,
-                const float4 *rcols, const float *bg, const int32_t *tile_base,
+                const uint64_t *keys, const void *entry_recs, const float4 *prim_cols,
+                const float *bg, const int32_t *tile_base,
                 const int32_t *dims, const int64_t *pix_base, float *out_c, float *out_a,
                 int32_t *last_ids, const float *render_alphas, const int32_t *last_in,
                 const float *v_out_c, const float *v_out_a, float *v_m2, float *v_cn,
@@ -944,8 +1045,10 @@ int scene_blend(int fwd, int32_t C, int64_t CN, int32_t n_buckets, int32_t tile_
     a.n_isects = cap;
     a.n_prims = CN;
     a.offsets = offsets;
-    a.recs = static_cast<const GeoRec *>(recs);
-    a.rcols = rcols;
+    a.keys = keys;
+    a.entry_recs = static_cast<const GeoRec *>(entry_recs);
+    a.prim_cols = prim_cols;
+    a.n_per_view = CN / C;
     a.bg = bg;
     a.status = status;
     a.v_tile_base = tile_base;

@@ -9,11 +9,12 @@
 //   1. scene_prim_fwd: one thread per (view, primitive) -- activations,
 //      rotation, D x D covariance, conditioning on the view ray (and time),
 //      EWA projection, tile counting into per-(view, tile) buckets;
-//   2. a device-side scan, bucketed emit and per-bucket sort that writes the
-//      blend's packed records directly (no flatten-id gather pass, no host
-//      round trip; the intersection count stays on the device);
+//   2. a device-side scan, bucketed emit and per-bucket sort of (depth,
+//      entry) keys (no host round trip; the intersection count stays on the
+//      device);
 //   3. the blend over a flattened (view, tile) work list whose views may have
-//      different resolutions;
+//      different resolutions, copying each batch of records from the
+//      per-entry tables by the sorted keys (no sorted copy of the records);
 //   4. scene_prim_bwd: one thread per (view, primitive) recomputes the forward
 //      chain and back-propagates blend gradients to the raw parameters.
 // Every launch is stream ordered with fixed grids, so a whole forward or
@@ -29,11 +30,12 @@
 
 namespace ubs {
 
-// raster.cu: the blend kernels in multi-view mode over sorted packed records
+// raster.cu: the blend kernels in multi-view mode, gathering each batch's
+// records from the per-entry tables through the sorted keys
 int scene_blend(int fwd, int32_t C, int64_t CN, int32_t n_buckets, int32_t tile_size,
                 const int32_t *offsets, const int32_t *order, const int64_t *T_dev, int64_t cap,
-                const void *recs,
-                const float4 *rcols, const float *bg, const int32_t *tile_base,
+                const uint64_t *keys, const void *entry_recs, const float4 *prim_cols,
+                const float *bg, const int32_t *tile_base,
                 const int32_t *dims, const int64_t *pix_base, float *out_c, float *out_a,
                 int32_t *last_ids, const float *render_alphas, const int32_t *last_in,
                 const float *v_out_c, const float *v_out_a, float *v_m2, float *v_cn,
@@ -219,7 +221,7 @@ template <int D> __global__ void scene_prim_fwd_kernel(SceneArgs a) {
     float4 *dst = reinterpret_cast<float4 *>(a.recs + idx);
     dst[0] = make_float4(r.x, r.y, r.opac, r.beta);
     dst[1] = make_float4(r.cxx, r.cxy, r.cyy, __int_as_float(r.gid));
-    if (v == 0) { // one colour row per primitive for the sorted-record gather
+    if (v == 0) { // one colour row per primitive, gathered by the blend
         if (a.color_mode == 1)
             a.cols_n[n] = make_float4(p.radius > 0 ? p.depth : 0.f, 0.f, 0.f, 0.f);
         else
@@ -281,36 +283,14 @@ __global__ void scene_emit_kernel(int64_t CN, int64_t N, const Rec *__restrict__
 
 
 // Sorted-entry writer of the fused path: the sort leaves each sorted key in
-// place; scene_gather_kernel then writes the blend's packed records.
+// place; the blend kernels gather each batch's records and colours from the
+// per-entry tables by the keys' low words.
 struct KeyWriter {
     uint64_t *keys;
     __device__ __forceinline__ void operator()(uint64_t key, int64_t pos, int64_t) const {
         keys[pos] = key;
     }
 };
-
-// One packed record and colour per sorted intersection, gathered by the
-// (view, primitive) index in the key's low word.  A grid-stride loop at full
-// occupancy keeps enough gathers in flight to hide their latency.
-__global__ void __launch_bounds__(256) scene_gather_kernel(const uint64_t *__restrict__ keys,
-                                                           const int64_t *T_dev, int64_t cap,
-                                                           const Rec *__restrict__ recs_in,
-                                                           const float4 *__restrict__ cols_n,
-                                                           int64_t N, Rec *__restrict__ recs_out,
-                                                           float4 *__restrict__ cols_out) {
-    const int64_t T = imin64(*T_dev, cap);
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < T; i += stride) {
-        const int64_t gid = (int64_t)(keys[i] & 0xffffffffu);
-        const float4 *src = reinterpret_cast<const float4 *>(recs_in + gid);
-        const float4 a = src[0], b = src[1];
-        const float4 c = cols_n[gid % N];
-        float4 *dst = reinterpret_cast<float4 *>(recs_out + i);
-        dst[0] = a;
-        dst[1] = b;
-        cols_out[i] = c;
-    }
-}
 
 template <int D> __global__ void scene_prim_bwd_kernel(SceneArgs a) {
     constexpr int K = D - 3;
@@ -443,8 +423,6 @@ struct SceneWs {
     int32_t *bucket_counts, *offsets, *cursor, *big_list, *order;
     int64_t *block_sums;
     uint64_t *keys, *scratch;
-    Rec *sorted;
-    float4 *cols;
     float4 *cols_n;
     float *grads; // v_m2 (2), v_cn (3), v_col (3), v_op, v_be per (view, primitive)
     size_t bytes;
@@ -472,8 +450,6 @@ SceneWs scene_ws(void *base, int32_t C, int64_t N, int32_t nb, int64_t cap) {
     w.block_sums = reinterpret_cast<int64_t *>(take(((nb + SCAN_TILE - 1) / SCAN_TILE + 1) * 8));
     w.keys = reinterpret_cast<uint64_t *>(take(cap * 8));
     w.scratch = reinterpret_cast<uint64_t *>(take(cap * 8));
-    w.sorted = reinterpret_cast<Rec *>(take(cap * sizeof(Rec)));
-    w.cols = reinterpret_cast<float4 *>(take(cap * 16));
     w.cols_n = reinterpret_cast<float4 *>(take((size_t)N * 16));
     w.grads = reinterpret_cast<float *>(take(CN * 10 * 4));
     w.bytes = o;
@@ -632,26 +608,13 @@ int ubs_scene_forward_masked(int32_t dim, int64_t N, const float *xyz, const flo
     if (int e = launch_bucket_sort(n_buckets, w.offsets, &w.hdr->total, capacity, w.keys,
                                    w.scratch, w.big_list, &w.hdr->n_big, wr, st))
         return e;
-    {
-        int dev = 0, sms = 152;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const unsigned grid = (unsigned)imin64(imin64((capacity + 255) / 256, (int64_t)sms * 8),
-                                               (int64_t)1 << 20);
-        UBS_TIMED("scene_gather", st,
-                  scene_gather_kernel<<<grid, 256, 0, st>>>(w.keys, &w.hdr->total, capacity,
-                                                            w.recs, w.cols_n, N, w.sorted,
-                                                            w.cols));
-        note_launch();
-        if (int e = check_launch("scene_gather")) return e;
-    }
     UBS_TIMED("bucket_order", st,
               bucket_order_kernel<<<1, 1024, 0, st>>>(w.offsets, &w.hdr->total, capacity,
                                                       n_buckets, w.order));
     note_launch();
     if (int e = check_launch("bucket_order")) return e;
     return scene_blend(1, C, CN, n_buckets, tile_size, w.offsets, w.order, &w.hdr->total, capacity,
-                       w.sorted, w.cols, backgrounds, tile_base, view_dims, pix_base,
+                       w.keys, w.recs, w.cols_n, backgrounds, tile_base, view_dims, pix_base,
                        render_colors, render_alphas, last_ids, nullptr, nullptr, nullptr, nullptr,
                        nullptr, nullptr, nullptr, nullptr, nullptr, &w.hdr->status, st);
 }
@@ -694,8 +657,8 @@ int ubs_scene_backward(int32_t dim, int64_t N, const float *xyz, const float *me
     if (cudaMemsetAsync(w.grads, 0, CN * 10 * 4, st) != cudaSuccess)
         return check_launch("scene_backward memset");
     if (int e = scene_blend(0, C, CN, n_buckets, tile_size, w.offsets, w.order, &w.hdr->total,
-                            capacity,
-                            w.sorted, w.cols, backgrounds, tile_base, view_dims, pix_base,
+                            capacity, w.keys, w.recs, w.cols_n, backgrounds, tile_base,
+                            view_dims, pix_base,
                             nullptr, nullptr, nullptr, render_alphas, last_ids, v_render_colors,
                             v_render_alphas, v_m2, v_cn, v_col, v_op, v_be, &w.hdr->status, st))
         return e;
