@@ -5,19 +5,23 @@
 // transmittance, exclusive termination at T <= 1e-4, back-to-front
 // transmittance recovery from 1 - render_alpha) follows the reference so that
 // images agree to FP32 rounding.  The data movement is new:
-//   * a pack pass writes one 32-byte geometry record (+16-byte colour record
-//     for <= 4 channels) per sorted intersection, so every tile reads its
-//     front-to-back list as one contiguous span;
-//   * each CTA streams its span through shared memory with bulk async copies
-//     (cp.async.bulk + mbarrier, double-buffered, bounded waits);
+//   * records are 32-byte geometry records (+16-byte colour records for <= 4
+//     channels).  The drop-in operators pack one per sorted intersection, so
+//     a tile's front-to-back list is one contiguous span that a CTA streams
+//     through shared memory with bulk async copies (cp.async.bulk + mbarrier,
+//     double-buffered, bounded waits).  The fused scene path keeps them as
+//     per-entry tables and every thread gathers its batch slots by the sorted
+//     keys (16-byte cp.async, arrival on the batch's mbarrier), so no sorted
+//     copy is ever written;
 //   * each thread owns two vertically adjacent pixels (a warp an 8x8 block),
 //     so record loads, loop control and the backward's warp reductions are
 //     shared by two pixels;
-//   * every batch, each record's ellipse bounding box is tested against the
-//     8x8-pixel footprint of every warp and turned into per-warp bitmasks by
-//     ballot, so a warp only visits records that can touch its pixels;
+//   * every batch, each record's ellipse is tested exactly against the
+//     8x8-pixel footprint of every warp and the results turned into per-warp
+//     bitmasks by ballot, so a warp only visits records that can touch its
+//     pixels;
 //   * the backward sums the 7 + channels gradients of a record over a warp with
-//     a transpose reduction (16 shuffles for 16 values), accumulates warps in
+//     transpose reductions (14 shuffles for 10 values), accumulates warps in
 //     shared memory and issues one global atomic per (tile, record, value).
 #include <cstdio>
 
