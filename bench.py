@@ -39,18 +39,25 @@ import torch  # noqa: E402
 
 METRIC = "render FPS and train it/s at 1M prims 1080p; serving p50/p99 ms vs plain form"
 N_PRIMS, DIM, WIDTH, HEIGHT, FOCAL, TILE = 1_000_000, 6, 1920, 1080, 1500.0, 16
-# Blend work units for the roofline.  Primary (the hot-path scope table's
-# definition): a (pixel, record) pair a per-pixel loop evaluates -- forward:
-# every record of the pixel's tile up to the one that ends it, else the whole
-# range, ~20 FP32 operations + 1 pow counted as 2 MUFU operations; backward:
-# records up to the pixel's last contributor, ~45 FP32 + 3 MUFU-class
-# operations (rasterize_to_pixels_fwd.cu:140-171, rasterize_to_pixels_bwd.cu:
-# 170-247).  Secondary: contributing pairs only, with this kernel's own
-# operation counts (FMA = 2).
-FWD_OPS_PER_EVAL_PAIR = 22
-BWD_OPS_PER_EVAL_PAIR = 48
-FWD_FLOP_PER_PAIR = 28
-BWD_FLOP_PER_PAIR = 77
+# Blend work for the roofline, counted from the reference's per-pair
+# arithmetic (rasterize_to_pixels_fwd.cu:139-171, rasterize_to_pixels_bwd.cu:
+# 158-247), 3 colour channels, no background.  FP32 FLOPs count a multiply or
+# an add as 1 and an FMA as 2 (the FP32 probe's convention); comparisons,
+# min/max and selects are not counted.  MUFU operations are counted apart and
+# set against the XU pipe's own probe.
+#   every pair a per-pixel loop evaluates: delta (2) + sigma (7 mul, 2 add) = 11
+#   forward, per contributing pair: 1 - sigma, beta log2, opacity x, 1 - alpha,
+#     T x, alpha T, 3 colour FMAs = 12 FLOPs; log2 + exp2 = 2 MUFU
+#   backward, per contributing pair: alpha chain 4, T and fac 2, v_rgb 3,
+#     v_alpha 15 + 3, v_sigma 5, v_conic 7, v_xy 10, v_opacity 1, v_beta 4,
+#     colour buffer 6 = 60 FLOPs; log2, exp2 and two reciprocals (1 / (1 - alpha),
+#     (1 - sigma)^(beta - 1) from the power) = 4 MUFU
+# Units: the forward's evaluated pairs (up to the terminating record, else the
+# tile's whole range) and the backward's pairs up to the last contributor --
+# the hot-path scope table's units -- plus the contributing pairs of both.
+PAIR_TEST_FLOP = 11
+FWD_CONTRIB_FLOP, FWD_CONTRIB_MUFU = 12, 2
+BWD_CONTRIB_FLOP, BWD_CONTRIB_MUFU = 60, 4
 # FP32 operations per (pixel, channel) of the SSIM training loss and its
 # gradient: two 11-tap passes (2 ops a tap) for the five windowed moments and
 # for the three derivative maps, plus ~40 for the products, the map, its
@@ -690,6 +697,24 @@ def fp32_peak(dev):
     return best
 
 
+def mufu_peak(dev):
+    """XU issue rate (T MUFU ops/s) from the library's probe, best of three."""
+    from ubs import _lib as L
+    import ctypes
+    ws = L.workspace(L.query("ubs_fp32_probe_workspace_bytes"), dev)
+    ops = ctypes.c_double(0)
+    best = 0.0
+    for it in (500, 500, 500):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        L.call("ubs_mufu_probe", it, L.ptr(ws), ws.numel(), ctypes.byref(ops), L.stream(dev))
+        e1.record()
+        e1.synchronize()
+        best = max(best, ops.value / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    return best
+
+
 def count_pairs(p, cam, ri, rj, bg, dev):
     """(contributing pairs, intersections, visible primitives, evaluated
     forward pairs, backward pairs) of one forward (device counters)."""
@@ -936,16 +961,42 @@ def run_config_d(dev, flush, rp):
     return out
 
 
-def run_serving(dev, rp, duration=3.0, rate=200.0):
+SLO_MS = 10.0
+SERVED_RATES = (200, 300, 400, 500, 600, 700, 800, 1000)
+PLAIN_RATES = (25, 50, 100, 150, 200, 300)
+
+
+def slo_sweep(run_at, rates, slo_ms=SLO_MS):
+    """Latency/throughput at each Poisson arrival rate; `best` is the rate
+    with the most frames/s among those whose p99 latency stays under slo_ms."""
+    rows = []
+    for rate in rates:
+        st = run_at(rate)
+        st["rate"] = rate
+        rows.append(st)
+    ok = [r for r in rows if r["p99_ms"] < slo_ms]
+    best = max(ok, key=lambda r: r["frames_per_s"]) if ok else None
+    return {"slo_p99_ms": slo_ms, "rates": rows,
+            "best": None if best is None else {k: best[k] for k in
+                                               ("rate", "frames_per_s", "p50_ms", "p99_ms",
+                                                "mean_batch")}}
+
+
+def run_serving(dev, rp, duration=3.0, rate=200.0, sweep_s=1.5):
     """Resident scenes of 500k, 1M and 3M 6-D primitives; Poisson requests at
-    `rate`/s with resolutions uniform over 640x480, 1280x720, 1920x1080."""
+    `rate`/s with resolutions uniform over 640x480, 1280x720, 1920x1080; then
+    a sweep of arrival rates per form for the highest throughput whose p99
+    latency stays under 10 ms."""
     from ubs import scene as S
     from ubs.serve import ServeConfig, Server, latency_stats, poisson_trace, run_plain
     sizes = {"s500k": 500_000, "s1m": 1_000_000, "s3m": 3_000_000}
     scenes = {k: S.synthetic_params(n, 6, seed=i, xyz_range=2.0, device=dev)
               for i, (k, n) in enumerate(sizes.items())}
     res = [(640, 480), (1280, 720), (1920, 1080)]
-    srv = Server(scenes, ServeConfig(max_slots=4, max_batch_views=8))
+    # a batch's estimated intersections are bounded so that one batch's device
+    # time stays a fraction of the latency target
+    cfg = ServeConfig(max_slots=4, max_batch_views=8, max_batch_isects=12_000_000)
+    srv = Server(scenes, cfg)
     srv.calibrate({k: S.orbit_view(7, 4.0, 1280, 720, 1000.0, 1000.0, device=dev) for k in scenes})
     trace = poisson_trace(rate, duration, list(scenes), res, seed=0, device=dev)
     srv.run(trace[:40], realtime=False)  # warm-up (allocator, kernels)
@@ -956,9 +1007,13 @@ def run_serving(dev, rp, duration=3.0, rate=200.0):
                        "%g req/s for %g s (%d requests), resolutions uniform over 640x480, "
                        "1280x720, 1920x1080, random radius-4 orbit cameras; latency = arrival "
                        "to image in pinned host memory" % (rate, duration, len(trace)),
-           "served": served, "served_saturated": saturated, "reruns": srv.reruns}
+           "served": served, "served_saturated": saturated, "reruns": srv.reruns,
+           "max_batch_isects": cfg.max_batch_isects}
     bg = torch.zeros(3, device=dev)
     ri, rj = S.rest_indices(6, dev)
+
+    def trace_at(r):
+        return poisson_trace(r, sweep_s, list(scenes), res, seed=int(r), device=dev)
 
     def dropin_one(r):
         with torch.no_grad():
@@ -968,6 +1023,11 @@ def run_serving(dev, rp, duration=3.0, rate=200.0):
     run_plain(dropin_one, trace[:20], realtime=False)
     out["plain_dropin"] = latency_stats(run_plain(dropin_one, trace, realtime=True))
     out["plain_dropin_saturated"] = latency_stats(run_plain(dropin_one, trace, realtime=False))
+    sweeps = {"served": slo_sweep(lambda r: latency_stats(srv.run(trace_at(r), realtime=True)),
+                                  SERVED_RATES),
+              "plain_dropin": slo_sweep(
+                  lambda r: latency_stats(run_plain(dropin_one, trace_at(r), realtime=True)),
+                  PLAIN_RATES)}
     if rp is not None:
         def ref_one(r):
             c = r.camera
@@ -980,6 +1040,25 @@ def run_serving(dev, rp, duration=3.0, rate=200.0):
         out["plain_ref_gpu"] = latency_stats(run_plain(ref_one, trace, realtime=True))
         out["plain_ref_gpu_saturated"] = latency_stats(run_plain(ref_one, trace,
                                                                  realtime=False))
+        sweeps["plain_ref_gpu"] = slo_sweep(
+            lambda r: latency_stats(run_plain(ref_one, trace_at(r), realtime=True)), PLAIN_RATES)
+    out["slo_sweep"] = sweeps
+    # the target: served frames/s under the latency bound over the plain
+    # one-request-per-launch form's, at its own best rate under the same bound
+    # and at its saturated (unbounded-latency) throughput
+    sb = sweeps["served"]["best"]
+    summary = {"served_fps_at_slo": sb and sb["frames_per_s"], "served_rate_at_slo": sb and sb["rate"]}
+    for form, sat in (("plain_dropin", "plain_dropin_saturated"),
+                      ("plain_ref_gpu", "plain_ref_gpu_saturated")):
+        if form not in sweeps:
+            continue
+        pb = sweeps[form]["best"]
+        summary[form] = {
+            "fps_at_slo": pb and pb["frames_per_s"], "rate_at_slo": pb and pb["rate"],
+            "saturated_fps": out[sat]["frames_per_s"],
+            "ratio_at_slo": (sb["frames_per_s"] / pb["frames_per_s"]) if (sb and pb) else None,
+            "ratio_vs_saturated": (sb["frames_per_s"] / out[sat]["frames_per_s"]) if sb else None}
+    out["slo_summary"] = summary
     return out
 
 
@@ -1153,6 +1232,38 @@ def run_cpu(steps, warmup, n_prims):
                       "1920x1080 frame (C++ oracle port, OpenMP)" % (FP, n_prims, F, cs.th)}
 
 
+def headline_summary(value, e2e_val, render_fps, d_ms, d_fwd_ms, ref_gpu, roofline, configs):
+    """The figures a reader compares, in one short dict: train it/s (graph
+    replay, end to end), render FPS, the drop-in operators' and the
+    reference kernels' plain form on the same GPU, the blend roofline
+    fractions, and configs C, D and E against the reference's plain form."""
+    def r3(x):
+        return None if x is None else round(float(x), 3)
+    out = {"train_it_s": r3(value), "e2e_it_s": r3(e2e_val), "render_fps": r3(render_fps),
+           "dropin_it_s": r3(1000.0 / d_ms), "dropin_render_fps": r3(1000.0 / d_fwd_ms)}
+    if ref_gpu and "value" in ref_gpu:
+        out["ref_gpu_it_s"] = r3(ref_gpu["value"])
+        out["ref_gpu_render_fps"] = r3(ref_gpu["render_fps"])
+        out["train_vs_ref_gpu"] = r3(value / ref_gpu["value"])
+        out["render_vs_ref_gpu"] = r3(render_fps / ref_gpu["render_fps"])
+    out["roofline"] = {"kernel": roofline["kernel"], "fp32_frac": r3(roofline["frac"]),
+                       "mufu_frac": r3(roofline["mufu"]["frac"]),
+                       "launch_ms": r3(roofline["launch_ms"])}
+    for name in ("C", "D"):
+        c = (configs or {}).get(name) or {}
+        if "ms_per_step" in c:
+            e = {"ms_per_step": r3(c["ms_per_step"])}
+            rg = c.get("ref_gpu_plain")
+            if rg:
+                e["ref_gpu_ms"] = r3(rg["ms_per_step"])
+                e["vs_ref_gpu"] = r3(rg["ms_per_step"] / c["ms_per_step"])
+            out["config_" + name] = e
+    e = (configs or {}).get("E") or {}
+    if "slo_summary" in e:
+        out["serving_p99_slo"] = e["slo_summary"]
+    return out
+
+
 # ------------------------------------------------------------------- main
 def main():
     args = parse()
@@ -1176,7 +1287,10 @@ def main():
                     "data": "synthetic (seeded, benchmark distributions)",
                     "config": {"workload": WORKLOAD, "n_prims": args.n_prims, "dim": DIM,
                                "width": WIDTH, "height": HEIGHT, "tile_size": TILE,
-                               "device": "host CPU"},
+                               "parallelism": "host CPU, %d threads" % r["cores"],
+                               "l2": "n/a (host CPU; each step a bounded sample)",
+                               "path": "C++ restatement of the reference's path (oracle), "
+                                       "OpenMP over tiles and primitives"},
                     "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
                     "e2e": {"value": r["value"], "unit": "it/s", "h2d_bytes_per_step": 0,
                             "d2h_bytes_per_step": 0}}
@@ -1426,28 +1540,34 @@ def main():
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except (OSError, ValueError):
         pass
+    peak_mufu = mufu_peak(dev)
     dominant = max(kernel_ms, key=kernel_ms.get)
     n_dom, t_dom = kernels[dominant]
     dom_ms = t_dom / n_dom
     is_bwd = dominant == "raster_bwd"
     units = bwd_pairs if is_bwd else eval_pairs
-    ops = BWD_OPS_PER_EVAL_PAIR if is_bwd else FWD_OPS_PER_EVAL_PAIR
-    achieved = units * ops / (dom_ms * 1e-3) / 1e12
-    flop_pp = BWD_FLOP_PER_PAIR if is_bwd else FWD_FLOP_PER_PAIR
-    contrib_achieved = pairs * flop_pp / (dom_ms * 1e-3) / 1e12
+    flop = units * PAIR_TEST_FLOP + pairs * (BWD_CONTRIB_FLOP if is_bwd else FWD_CONTRIB_FLOP)
+    mufu = pairs * (BWD_CONTRIB_MUFU if is_bwd else FWD_CONTRIB_MUFU)
+    fp32_ach = flop / (dom_ms * 1e-3) / 1e12
+    mufu_ach = mufu / (dom_ms * 1e-3) / 1e12
+    fp32_frac = fp32_ach / peak_fp32 if peak_fp32 else None
+    mufu_frac = mufu_ach / peak_mufu if peak_mufu else None
     roofline = {
         "kernel": dominant, "bound": "fp32",
-        "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s",
-        "frac": achieved / peak_fp32 if peak_fp32 else None,
+        "achieved": fp32_ach, "peak": peak_fp32, "unit": "TFLOP/s (FP32, FMA = 2 FLOPs)",
+        "frac": fp32_frac,
         "traffic": read_profile_traffic(dominant),
-        "algorithmic_work": "%d %s pairs x %d operations (FP32 + MUFU) per launch" % (
-            units, "backward (records up to each pixel's last contributor)" if is_bwd else
-            "evaluated", ops),
-        "contributing_pairs": {"pairs": pairs, "ops_per_pair": flop_pp,
-                               "achieved": contrib_achieved,
-                               "frac": contrib_achieved / peak_fp32 if peak_fp32 else None},
-        "peak_source": "measured: FP32 FMA probe kernel timed in this run (MEASURED_PEAKS.json "
-                       "has HBM %s GB/s and bf16 only)" % peaks.get("hbm_gbs", "n/a"),
+        "algorithmic_work": "%d %s pairs x %d FLOPs + %d contributing pairs x %d FLOPs = %.2f "
+                            "GFLOP per launch" % (
+                                units, "backward (up to each pixel's last contributor)" if is_bwd
+                                else "evaluated", PAIR_TEST_FLOP, pairs,
+                                BWD_CONTRIB_FLOP if is_bwd else FWD_CONTRIB_FLOP, flop / 1e9),
+        "mufu": {"ops_per_launch": mufu, "achieved": mufu_ach, "peak": peak_mufu,
+                 "unit": "T MUFU ops/s", "frac": mufu_frac,
+                 "peak_source": "XU probe kernel (exp2 chains) timed in this run"},
+        "peak_source": "FP32 FMA probe kernel timed in this run (MEASURED_PEAKS.json has HBM "
+                       "%s GB/s and bf16 only; the blend has no dense contraction)"
+                       % peaks.get("hbm_gbs", "n/a"),
         "launch_ms": dom_ms,
         "timing": "CUDA events on the launching stream around each launch (graph event "
                   "nodes), every replay of the timed region",
@@ -1521,7 +1641,6 @@ def main():
                              "per-step CUDA events",
                        "path": "fused scene render (ubs.render.Renderer), whole step "
                                "replayed as one CUDA graph (ubs.render.GraphedStep)"},
-            "render_fps": 1000.0 / fwd_ms,
             "e2e": {"value": e2e_val, "unit": "it/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": 4, "ms_per_step": e2e_ms,
                     "how": "ubs.render.HostFedStep: parameters and target copied from pinned "
@@ -1534,24 +1653,27 @@ def main():
             "launches_per_step": int(launches) // max(1, args.steps),
             "roofline": roofline,
             "cpu_baseline": cpu,
-            "ref_gpu": ref_gpu,
+            "clocks": clocks.summary(clocks.marks.get("t0", 0), clocks.marks.get("t1", 0)),
+            "configs": configs,
             "train_iteration": train_iter,
             "loss": loss_res,
             "densify": densify,
             "scene_file": scene_file,
             "viewer": viewer,
-            "eager": {"value": 1000.0 / eager_ms, "unit": "it/s", "ms_per_step": eager_ms,
-                      "what": "the same fused step launched kernel by kernel (no graph)"},
-            "dropin": {"value": 1000.0 / d_ms, "unit": "it/s", "ms_per_step": d_ms,
-                       "render_fps": 1000.0 / d_fwd_ms, "kernels_ms_per_step": d_kernels,
-                       "what": "the same step through the drop-in gsplat operators"},
-            "clocks": clocks.summary(clocks.marks.get("t0", 0), clocks.marks.get("t1", 0)),
             "kernels_ms_per_step": {k: round(v, 4) for k, v in
                                     sorted(kernel_ms.items(), key=lambda x: -x[1])},
             "isects": n_isects, "visible": n_visible, "pairs": pairs,
             "evaluated_pairs": eval_pairs, "backward_pairs": bwd_pairs,
             "wall_s_timed": wall,
-            "configs": configs,
+            "eager": {"value": 1000.0 / eager_ms, "unit": "it/s", "ms_per_step": eager_ms,
+                      "what": "the same fused step launched kernel by kernel (no graph)"},
+            "dropin": {"value": 1000.0 / d_ms, "unit": "it/s", "ms_per_step": d_ms,
+                       "render_fps": 1000.0 / d_fwd_ms, "kernels_ms_per_step": d_kernels,
+                       "what": "the same step through the drop-in gsplat operators"},
+            "ref_gpu": ref_gpu,
+            # the headline figures last, where a reader of the line's tail finds them
+            "summary": headline_summary(value, e2e_val, 1000.0 / fwd_ms, d_ms, d_fwd_ms,
+                                        ref_gpu, roofline, configs),
         }
         print(json.dumps(line), flush=True)
     if world > 1:

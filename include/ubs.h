@@ -64,6 +64,13 @@ int ubs_profile_result(int32_t i, const char **name, int64_t *launches, double *
 size_t ubs_fp32_probe_workspace_bytes(void);
 int ubs_fp32_probe(int32_t iters, void *workspace, size_t workspace_bytes, double *flops,
                    void *stream);
+/* XU (multi-function unit) issue-rate probe (no reference counterpart): the
+ * same launch shape running chains of base-2 exponentials; *ops receives the
+ * launch's MUFU operation count, the denominator for the blend kernels'
+ * transcendental work (log2 / exp2 / reciprocal).  Workspace as the FP32
+ * probe's. */
+int ubs_mufu_probe(int32_t iters, void *workspace, size_t workspace_bytes, double *ops,
+                   void *stream);
 
 /* ------------------------------------------------------------------ a2 ---
  * R = I + A(a01, a02, a12): submodules/gsplat/cuda/_wrapper.py:34
@@ -144,6 +151,11 @@ int ubs_projection_bwd(int32_t C, int64_t N, const float *means, const float *co
  * Step 1 (synchronises the stream, like the reference's .item()):
  *   tiles_per_gauss [C,N], isect_offsets [C,tile_height,tile_width] and the
  *   intersection count.  Workspace: ubs_isect_count_workspace_bytes().
+ *   It blocks the host because the drop-in operator returns isect_ids /
+ *   flatten_ids as tensors whose length is the count, so the caller must
+ *   know it before it can allocate them (the reference reads it with .item()
+ *   at the same point, isect_tiles.cu:181).  The fused scene render below
+ *   keeps the count on the device and never synchronises.
  * Step 2: isect_ids [n_isects] int64 (cam | tile | depth bits) and
  *   flatten_ids [n_isects] int32, sorted like the reference's stable radix sort
  *   when sort != 0, else in the reference's generation order.  Workspace:
@@ -455,6 +467,30 @@ int ubs_scene_forward(int32_t dim, int64_t N, const float *xyz, const float *mea
  * there -- the reference's meta["radii"] / meta["depths"]. */
 int ubs_scene_workspace_offsets(int32_t C, int64_t N, int32_t n_buckets, int64_t capacity,
                                 int64_t *radius_offset, int64_t *depth_offset);
+/* Byte offsets, inside a forward's workspace, of what the forward leaves
+ * there (sections[i] for i < n_sections, in the order of the UBS_SCENE_WS_*
+ * indices):
+ *   RECORDS  per (view, primitive) 32-B records {x, y, opacity, beta, conic
+ *            xx, xy, yy, entry id} -- meta["means2d"] / ["conics"] of the
+ *            reference (fully_fused_projection_fwd.cu:20-177), zeros where the
+ *            radius is 0;
+ *   RADII    int32 [C, N], DEPTHS float [C, N] (as ubs_scene_workspace_offsets);
+ *   BUCKET_STARTS  int32 [n_buckets]: first intersection of bucket b =
+ *            tile_base[view] + tile (an exclusive scan of the counts; the last
+ *            bucket ends at the intersection total, ubs_scene_stats);
+ *   KEYS     uint64 [total], sorted within each bucket: float bits of the
+ *            depth << 32 | view * N + primitive.
+ * Per view, tile << 32 | key >> 32 is the reference's single-camera isect id
+ * and the low word minus view * N its flatten id, in the same order
+ * (isect_tiles.cu:82-96, 232-280, 287-367). */
+#define UBS_SCENE_WS_RECORDS 0
+#define UBS_SCENE_WS_RADII 1
+#define UBS_SCENE_WS_DEPTHS 2
+#define UBS_SCENE_WS_BUCKET_STARTS 3
+#define UBS_SCENE_WS_KEYS 4
+#define UBS_SCENE_WS_N_SECTIONS 5
+int ubs_scene_workspace_layout(int32_t C, int64_t N, int32_t n_buckets, int64_t capacity,
+                               int64_t *sections, int32_t n_sections);
 /* ubs_scene_forward with two viewer options (scene/beta_model.py:725-831):
  * prim_mask (device uint8 [N], or NULL) leaves out primitives whose entry is
  * 0 -- the same image as rendering the masked subset, as the reference's

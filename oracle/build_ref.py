@@ -12,7 +12,8 @@ The reference's host code (pybind/torch wrappers, cub sort) is not built: its
 kernels are launched with the reference's own launch shapes, and its cub sort
 is replaced by a stable sort, which defines the same order.
 
-Usage:  python oracle/build_ref.py [/path/to/reference]
+Usage:  python oracle/build_ref.py /path/to/reference
+        (or set UBS_REFERENCE_ROOT to the checkout and omit the argument)
 """
 import concurrent.futures as cf
 import os
@@ -41,7 +42,17 @@ def csrc_dir(ref_root):
     return os.path.join(ref_root, "submodules", "gsplat", "cuda", "csrc")
 
 
-def build(ref_root="/root/reference", force=False, verbose=False):
+def reference_root(arg=None):
+    """The reference checkout: the argument, else $UBS_REFERENCE_ROOT, else None."""
+    return arg or os.environ.get("UBS_REFERENCE_ROOT") or None
+
+
+def build(ref_root=None, force=False, verbose=False):
+    """Compile the cubins from the checkout at ref_root (or $UBS_REFERENCE_ROOT);
+    returns the output folder, or None when no checkout is given or found."""
+    ref_root = reference_root(ref_root)
+    if ref_root is None:
+        return None
     csrc = csrc_dir(ref_root)
     if not os.path.isdir(csrc):
         return None
@@ -78,4 +89,7 @@ def build(ref_root="/root/reference", force=False, verbose=False):
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    print(build(args[0] if args else "/root/reference", force="--force" in sys.argv, verbose=True))
+    root = reference_root(args[0] if args else None)
+    if root is None:
+        sys.exit("usage: build_ref.py /path/to/reference (or set UBS_REFERENCE_ROOT)")
+    print(build(root, force="--force" in sys.argv, verbose=True))

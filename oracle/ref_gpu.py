@@ -402,4 +402,5 @@ class RefPipeline:
         colors = p["rgb"].expand(1, -1, -1)
         oc, oa = self.Raster.apply(m2, cn, colors, op, be, background.unsqueeze(0), W, H,
                                    tile_size, offs, fl)
-        return oc.permute(0, 3, 1, 2)[0], oa, dict(radii=radii, isect_ids=ids, flatten_ids=fl)
+        return oc.permute(0, 3, 1, 2)[0], oa, dict(radii=radii, isect_ids=ids, flatten_ids=fl,
+                                                   isect_offsets=offs[0])

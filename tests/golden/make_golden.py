@@ -9,7 +9,7 @@ stores inputs plus outputs (and autograd gradients) as .npz files next to this
 script.  The blend has no CPU implementation in the reference (it needs the CUDA
 extension and nerfacc), so blend parity is pinned on the GPU instead.
 
-Usage:  python tests/golden/make_golden.py [/path/to/reference]
+Usage:  python tests/golden/make_golden.py /path/to/reference
 """
 import os
 import sys
@@ -18,7 +18,9 @@ import numpy as np
 import torch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("UBS_REFERENCE_ROOT")
+if not REF:
+    sys.exit("usage: %s /path/to/reference (or set UBS_REFERENCE_ROOT)" % sys.argv[0])
 sys.path.insert(0, os.path.join(REF, "submodules"))
 from gsplat.cuda import _torch_impl as ti  # noqa: E402
 

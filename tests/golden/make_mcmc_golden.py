@@ -10,7 +10,7 @@ torch.optim.Adam carrying non-zero moments, runs relocate_gs and add_new_gs,
 records the indices torch.multinomial drew (by wrapping _sample_alives) and
 stores inputs, drawn indices and outputs in mcmc.npz next to this script.
 
-Usage:  python tests/golden/make_mcmc_golden.py [/path/to/reference]
+Usage:  python tests/golden/make_mcmc_golden.py /path/to/reference
 """
 import importlib.util
 import os
@@ -21,7 +21,9 @@ import numpy as np
 import torch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("UBS_REFERENCE_ROOT")
+if not REF:
+    sys.exit("usage: %s /path/to/reference (or set UBS_REFERENCE_ROOT)" % sys.argv[0])
 NAMES = ["xyz", "mean", "rgb", "opacity", "beta", "scale", "l_triangle"]
 
 

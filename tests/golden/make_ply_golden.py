@@ -2,7 +2,7 @@
 scene/beta_model.py:286-296), evaluated by the reference's own method for
 6-D and 7-D models, stored as ply_attributes.json next to this script.
 
-Usage:  python tests/golden/make_ply_golden.py [/path/to/reference]
+Usage:  python tests/golden/make_ply_golden.py /path/to/reference
 """
 import json
 import os

@@ -9,7 +9,7 @@ float64 (the reference builds its window in float32 either way), takes the
 autograd gradients (stored as float32) w.r.t. the rendered image, and stores everything in
 ssim.npz next to this script.
 
-Usage:  python tests/golden/make_ssim_golden.py [/path/to/reference]
+Usage:  python tests/golden/make_ssim_golden.py /path/to/reference
 """
 import importlib.util
 import os
@@ -19,7 +19,9 @@ import numpy as np
 import torch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("UBS_REFERENCE_ROOT")
+if not REF:
+    sys.exit("usage: %s /path/to/reference (or set UBS_REFERENCE_ROOT)" % sys.argv[0])
 spec = importlib.util.spec_from_file_location("ref_loss_utils",
                                               os.path.join(REF, "utils", "loss_utils.py"))
 lu = importlib.util.module_from_spec(spec)

@@ -89,3 +89,16 @@ def test_every_request_is_served_exactly_once():
         served += [r.rid for r in b[1]]
         inflight.append(b)
     assert sorted(served) == list(range(200)) and s.in_flight_bytes == 0
+
+
+def test_intersection_bound_caps_a_batch_but_never_starves_it():
+    # 1 intersection per pixel: 100x100 views of 10,000 each; a 25,000 bound
+    # takes two views per batch, and a lone view larger than the bound still goes
+    cfg = ServeConfig(max_slots=4, max_batch_views=8, mem_budget=1 << 40, margin=1.0,
+                      max_batch_isects=25_000)
+    s = make(cfg)
+    s.arrive(reqs([("a", 100, 100)] * 3 + [("b", 300, 300)]))
+    assert [r.rid for r in s.next_batch()[1]] == [0, 1]
+    assert [r.rid for r in s.next_batch()[1]] == [2]
+    assert [r.rid for r in s.next_batch()[1]] == [3]
+    assert s.next_batch() is None

@@ -31,6 +31,22 @@ __global__ void fp32_probe_kernel(int iters, float *out) {
     out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
 }
 
+// XU (MUFU) issue-rate probe: 8 independent chains of base-2 exponentials per
+// thread (exp2f is one MUFU.EX2 under fast math); the chain values stay in
+// (0, 1] so no special-case path runs.
+__global__ void mufu_probe_kernel(int iters, float *out) {
+    float a0 = -1e-3f * (threadIdx.x & 7), a1 = a0 - 0.01f, a2 = a0 - 0.02f, a3 = a0 - 0.03f;
+    float a4 = a0 - 0.04f, a5 = a0 - 0.05f, a6 = a0 - 0.06f, a7 = a0 - 0.07f;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            a0 = -exp2f(a0); a1 = -exp2f(a1); a2 = -exp2f(a2); a3 = -exp2f(a3);
+            a4 = -exp2f(a4); a5 = -exp2f(a5); a6 = -exp2f(a6); a7 = -exp2f(a7);
+        }
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
 int set_error(int code, const char *fmt, ...) {
     va_list ap;
     va_start(ap, fmt);
@@ -150,6 +166,22 @@ int ubs_fp32_probe(int32_t iters, void *workspace, size_t workspace_bytes, doubl
     ubs::note_launch();
     if (flops) *flops = 2.0 * 8 * 16 * (double)iters * sms * 8 * 256;
     return ubs::check_launch("fp32_probe");
+}
+
+int ubs_mufu_probe(int32_t iters, void *workspace, size_t workspace_bytes, double *ops,
+                   void *stream) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return ubs::check_launch("mufu_probe device query");
+    const size_t need = (size_t)sms * 8 * 256 * sizeof(float);
+    if (iters <= 0 || !workspace || workspace_bytes < need)
+        return ubs::set_error(UBS_ERR_INVALID, "mufu_probe: need iters > 0 and %zu B", need);
+    ubs::mufu_probe_kernel<<<sms * 8, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        iters, static_cast<float *>(workspace));
+    ubs::note_launch();
+    if (ops) *ops = 8.0 * 16 * (double)iters * sms * 8 * 256;
+    return ubs::check_launch("mufu_probe");
 }
 
 int ubs_profile_start(int32_t max_launches) {

@@ -81,21 +81,13 @@ __global__ void __launch_bounds__(ROW_BLOCK) covar_fwd_kernel(int64_t n, const f
                     else covar[i * 9 + r * 3 + c] = v;
                 }
         } else {
+            float V[D * D];
+            covar_from_L<D>(L, V);
 #pragma unroll
-            for (int r = 0; r < D; ++r)
-#pragma unroll
-                for (int c = 0; c <= r; ++c) {
-                    float acc = 0.f;
-#pragma unroll
-                    for (int k = 0; k < D; ++k) acc += L[r * D + k] * L[c * D + k];
-                    if (STAGE) {
-                        full.at(t, r * D + c) = acc;
-                        full.at(t, c * D + r) = acc;
-                    } else {
-                        covar[i * D * D + r * D + c] = acc;
-                        covar[i * D * D + c * D + r] = acc;
-                    }
-                }
+            for (int k = 0; k < D * D; ++k) {
+                if (STAGE) full.at(t, k) = V[k];
+                else covar[i * D * D + k] = V[k];
+            }
         }
     }
     if (!STAGE) return;

@@ -619,6 +619,45 @@ __device__ __forceinline__ void cond_backward(const float *m, const float *V, fl
 }
 
 // ------------------------------------------------------ D x D covariance
+// V = L L^T (V: [D*D] row-major, both triangles) with the summation shapes of
+// rot_scale_l_triangle_to_covar_fwd.cu:37-183, so that the covariance -- and
+// with it the conditioned mean and the projected depth that keys the sort --
+// rounds identically: each spatial 3x3 entry is one three-term expression
+// (the way it is written decides which product the compiler fuses into an
+// FMA); a diagonal entry of rows >= 3 starts from the rounded squared scale
+// and adds the row's lower-triangle squares by FMA; every other entry
+// accumulates over k in ascending order (L's zeros add nothing).
+template <int D> __device__ __forceinline__ void covar_from_L(const float *L, float *V) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c <= r; ++c) {
+            const float v = L[r * D] * L[c * D] + L[r * D + 1] * L[c * D + 1] +
+                            L[r * D + 2] * L[c * D + 2];
+            V[r * D + c] = v;
+            V[c * D + r] = v;
+        }
+#pragma unroll
+    for (int r = 3; r < D; ++r) {
+#pragma unroll
+        for (int c = 0; c < r; ++c) {
+            float acc = 0.f;
+#pragma unroll
+            for (int k = 0; k < D; ++k) acc += L[r * D + k] * L[c * D + k];
+            V[r * D + c] = acc;
+            V[c * D + r] = acc;
+        }
+        // the reference adds each square to a running sum that starts from
+        // the rounded s_r^2 (its loop fuses the added product, never s_r^2):
+        // an explicitly rounded first product keeps the compiler from
+        // fusing it into the first addition instead
+        float sq = __fmul_rn(L[r * D + r], L[r * D + r]);
+#pragma unroll
+        for (int k = 0; k < r; ++k) sq += L[r * D + k] * L[r * D + k];
+        V[r * D + r] = sq;
+    }
+}
+
 // L: [D*D] row-major factor of rot_scale_l_triangle_to_covar_fwd.cu:8-188
 template <int D>
 __device__ __forceinline__ void build_L(const float *R, const float *s, const float *lrest,

@@ -41,9 +41,16 @@ int scene_blend(int fwd, int32_t C, int64_t CN, int32_t n_buckets, int32_t tile_
                 const float *v_out_c, const float *v_out_a, float *v_m2, float *v_cn,
                 float *v_col, float *v_op, float *v_be, uint32_t *status, cudaStream_t st);
 
+// scene_act.cu (compiled with IEEE math): activated scales, betas and
+// opacities, act = [N, D] | [N, D - 2] | [N]
+int launch_scene_act(int64_t N, int D, const float *scale, const float *beta, const float *opac,
+                     float *act, cudaStream_t st);
+
 namespace {
 
 constexpr int kTileMaxViews = 1 << 16;
+// floats per primitive of the activation section (D + D - 2 + 1, D <= 7)
+constexpr int kActPerPrim = 13;
 
 struct __align__(16) Rec {
     float x, y, opac, beta;
@@ -67,6 +74,7 @@ struct SceneArgs {
     const float *viewmats, *intr, *centers, *times;
     const int32_t *dims, *tile_base;
     float tile_size, eps2d, near_p, far_p, radius_clip;
+    const float *act;         // activated scale [N,D] | beta [N,D-2] | opacity [N]
     const uint8_t *prim_mask; // optional: primitives with 0 are not rendered
     int color_mode;           // 0: rgb; 1: depth in channel 0 (one view, forward only)
     // outputs / workspace
@@ -82,10 +90,6 @@ struct SceneArgs {
     int exact;
 };
 
-__device__ __forceinline__ float softplus_f(float x) {
-    // log(1 + e^x), overflow-safe
-    return x > 20.f ? x : log1pf(expf(x));
-}
 __device__ __forceinline__ float sigmoid_f(float x) { return 1.f / (1.f + expf(-x)); }
 
 __device__ __forceinline__ Cam view_cam(const SceneArgs &a, int v) {
@@ -104,6 +108,23 @@ __device__ __forceinline__ Cam view_cam(const SceneArgs &a, int v) {
     return c;
 }
 
+// The conditioning query of the reference model, view_dir / |view_dir| with
+// view_dir = xyz - camera_center (scene/beta_model.py:676-678), rounded as
+// PyTorch's kernels round it: IEEE subtraction, the norm as PyTorch's
+// reduction sums the three squares (pairwise, (x0^2 + x2^2) + x1^2), IEEE
+// square root and division.  Explicitly rounded intrinsics keep fast math
+// from contracting or approximating any step.
+__device__ __forceinline__ void view_direction(const float *xyz, const float *center, float *q) {
+    const float d0 = __fsub_rn(xyz[0], center[0]);
+    const float d1 = __fsub_rn(xyz[1], center[1]);
+    const float d2 = __fsub_rn(xyz[2], center[2]);
+    const float ss = __fadd_rn(__fadd_rn(__fmul_rn(d0, d0), __fmul_rn(d2, d2)), __fmul_rn(d1, d1));
+    const float nrm = __fsqrt_rn(ss);
+    q[0] = __fdiv_rn(d0, nrm);
+    q[1] = __fdiv_rn(d1, nrm);
+    q[2] = __fdiv_rn(d2, nrm);
+}
+
 // Forward state of one (view, primitive), shared by both kernels.
 template <int D> struct PrimFwd {
     static constexpr int K = D - 3;
@@ -118,18 +139,78 @@ template <int D> struct PrimFwd {
     float om[3], oV[9], oo; // conditioned mean, covariance, opacity
 };
 
+// One primitive's parameter rows: xyz (3), mean (K), activated scale (D),
+// l_triangle (NL), activated beta (D - 2), and its activated opacity.
+struct PrimRows {
+    const float *xyz, *mean, *s, *lt, *b;
+    float o;
+};
+
+// Floats of one warp's parameter stage: the rows of 32 primitives.
+template <int D> constexpr int stage_floats() {
+    return 32 * (3 + (D - 3) + D + D * (D - 1) / 2 + (D - 2));
+}
+
+// The rows of the 32 consecutive primitives [n0, n0 + 32) of a [N, W] array
+// are one contiguous span: the warp reads it with W coalesced 128-byte loads
+// into its stage, and each lane then reads its own row from shared memory
+// (after the caller's __syncwarp; no CTA barrier, so warps keep overlapping).
+template <int W>
+__device__ __forceinline__ const float *stage_rows(const float *__restrict__ src, int64_t n0,
+                                                   float *st, int lane) {
+    const float *p = src + n0 * W;
+#pragma unroll
+    for (int k = 0; k < W; ++k) st[k * 32 + lane] = __ldg(p + k * 32 + lane);
+    return st + lane * W;
+}
+
+// Rows of primitive n: staged for the warp when its 32 entries are 32
+// consecutive primitives of one view (every warp but the one straddling a
+// view boundary or the end), else read in place.  Returns whether staged;
+// the caller syncs the warp before reading staged rows.
 template <int D>
-__device__ __forceinline__ void prim_forward(const SceneArgs &a, int64_t n, int v,
+__device__ __forceinline__ bool prim_rows(const SceneArgs &a, int64_t idx, int64_t n, int lane,
+                                          float *stage, PrimRows &r) {
+    constexpr int K = D - 3, NL = D * (D - 1) / 2;
+    const float *act_s = a.act, *act_b = a.act + a.N * D, *act_o = act_b + a.N * (D - 2);
+    const int64_t w0 = idx - lane, n0 = n - lane;
+    const bool staged = w0 + 32 <= (int64_t)a.C * a.N && n0 >= 0 && n0 + 32 <= a.N;
+    if (__all_sync(0xffffffffu, staged)) {
+        float *st = stage;
+        r.xyz = stage_rows<3>(a.xyz, n0, st, lane);
+        st += 32 * 3;
+        r.mean = stage_rows<K>(a.mean, n0, st, lane);
+        st += 32 * K;
+        r.s = stage_rows<D>(act_s, n0, st, lane);
+        st += 32 * D;
+        r.lt = stage_rows<NL>(a.ltri, n0, st, lane);
+        st += 32 * NL;
+        r.b = stage_rows<D - 2>(act_b, n0, st, lane);
+        r.o = act_o[n];
+        return true;
+    }
+    if (n >= 0 && n < a.N) {
+        r.xyz = a.xyz + n * 3;
+        r.mean = a.mean + n * K;
+        r.s = act_s + n * D;
+        r.lt = a.ltri + n * NL;
+        r.b = act_b + n * (D - 2);
+        r.o = act_o[n];
+    }
+    return false;
+}
+
+template <int D>
+__device__ __forceinline__ void prim_forward(const SceneArgs &a, const PrimRows &rw, int v,
                                              PrimFwd<D> &f) {
     constexpr int K = D - 3;
     constexpr int NL = D * (D - 1) / 2;
-    float raw_s[D], lt[NL];
+    float lt[NL];
+    // activations as the reference's PyTorch kernels round them (scene_act.cu)
 #pragma unroll
-    for (int k = 0; k < D; ++k) raw_s[k] = a.scale[n * D + k];
+    for (int k = 0; k < NL; ++k) lt[k] = rw.lt[k];
 #pragma unroll
-    for (int k = 0; k < NL; ++k) lt[k] = a.ltri[n * NL + k];
-#pragma unroll
-    for (int k = 0; k < D; ++k) f.s[k] = softplus_f(raw_s[k]);
+    for (int k = 0; k < D; ++k) f.s[k] = rw.s[k];
     // L: top-left R diag(s[0:3]) with R = I + A(a01, a02, a12); L[r][r] = s[r] (r >= 3);
     // rest entries row-major below the diagonal
     const float R[9] = {1.f, lt[0], lt[1], -lt[0], 1.f, lt[2], -lt[1], -lt[2], 1.f};
@@ -146,31 +227,18 @@ __device__ __forceinline__ void prim_forward(const SceneArgs &a, int64_t n, int 
         for (int c = 0; c < r; ++c) f.L[r * D + c] = lt[m++];
         f.L[r * D + r] = f.s[r];
     }
+    covar_from_L<D>(f.L, f.V);
 #pragma unroll
-    for (int r = 0; r < D; ++r)
+    for (int k = 0; k < 3; ++k) f.m[k] = rw.xyz[k];
 #pragma unroll
-        for (int c = 0; c <= r; ++c) {
-            float acc = 0.f;
+    for (int k = 0; k < K; ++k) f.m[3 + k] = rw.mean[k];
+    f.o = rw.o;
+    f.b0 = rw.b[0];
 #pragma unroll
-            for (int k = 0; k < D; ++k) acc += f.L[r * D + k] * f.L[c * D + k];
-            f.V[r * D + c] = acc;
-            f.V[c * D + r] = acc;
-        }
-#pragma unroll
-    for (int k = 0; k < 3; ++k) f.m[k] = a.xyz[n * 3 + k];
-#pragma unroll
-    for (int k = 0; k < K; ++k) f.m[3 + k] = a.mean[n * K + k];
-    f.o = sigmoid_f(a.opac[n]);
-    f.b0 = 4.f * expf(a.beta[n * (D - 2)]);
-#pragma unroll
-    for (int k = 0; k < K; ++k) f.b[k] = 4.f * expf(a.beta[n * (D - 2) + 1 + k]);
+    for (int k = 0; k < K; ++k) f.b[k] = rw.b[1 + k];
     // view direction query (+ timestamp for the 7-D model)
     const float *cc = a.centers + v * 3;
-    const float d0 = f.m[0] - cc[0], d1 = f.m[1] - cc[1], d2 = f.m[2] - cc[2];
-    const float inv = 1.f / sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
-    f.q[0] = d0 * inv;
-    f.q[1] = d1 * inv;
-    f.q[2] = d2 * inv;
+    view_direction(f.m, cc, f.q);
     if (K == 4) f.q[3 % K] = a.times[v];
     cond_forward<K>(f.m, f.V, f.o, f.b, f.q, f.om, f.oV, &f.oo);
 }
@@ -185,13 +253,19 @@ __device__ __forceinline__ M3 upper_sym(const float *oV) {
     return S;
 }
 
-template <int D> __global__ void scene_prim_fwd_kernel(SceneArgs a) {
+constexpr int PRIM_THREADS = 128;
+
+template <int D> __global__ void __launch_bounds__(PRIM_THREADS) scene_prim_fwd_kernel(SceneArgs a) {
+    __shared__ float stage[PRIM_THREADS / 32][stage_floats<D>()];
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)a.C * a.N) return;
+    const int lane = threadIdx.x & 31;
     const int v = (int)(idx / a.N);
     const int64_t n = idx - (int64_t)v * a.N;
+    PrimRows rows;
+    if (prim_rows<D>(a, idx, n, lane, stage[threadIdx.x >> 5], rows)) __syncwarp();
+    if (idx >= (int64_t)a.C * a.N) return;
     PrimFwd<D> f;
-    prim_forward<D>(a, n, v, f);
+    prim_forward<D>(a, rows, v, f);
     const Cam cam = view_cam(a, v);
     const uint32_t W = (uint32_t)a.dims[v * 4], H = (uint32_t)a.dims[v * 4 + 1];
     const uint32_t TW = (uint32_t)a.dims[v * 4 + 2], TH = (uint32_t)a.dims[v * 4 + 3];
@@ -292,13 +366,17 @@ struct KeyWriter {
     }
 };
 
-template <int D> __global__ void scene_prim_bwd_kernel(SceneArgs a) {
+template <int D> __global__ void __launch_bounds__(PRIM_THREADS) scene_prim_bwd_kernel(SceneArgs a) {
     constexpr int K = D - 3;
     constexpr int NL = D * (D - 1) / 2;
+    __shared__ float stage[PRIM_THREADS / 32][stage_floats<D>()];
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)a.C * a.N) return;
+    const int lane = threadIdx.x & 31;
     const int v = (int)(idx / a.N);
     const int64_t n = idx - (int64_t)v * a.N;
+    PrimRows rows;
+    if (prim_rows<D>(a, idx, n, lane, stage[threadIdx.x >> 5], rows)) __syncwarp();
+    if (idx >= (int64_t)a.C * a.N) return;
     const bool direct = a.C == 1; // one view: plain stores, else atomics into zeroed grads
     if (a.radius[idx] <= 0) {
         if (direct) {
@@ -319,7 +397,7 @@ template <int D> __global__ void scene_prim_bwd_kernel(SceneArgs a) {
         return;
     }
     PrimFwd<D> f;
-    prim_forward<D>(a, n, v, f);
+    prim_forward<D>(a, rows, v, f);
     const Cam cam = view_cam(a, v);
     const uint32_t W = (uint32_t)a.dims[v * 4], H = (uint32_t)a.dims[v * 4 + 1];
     // projection VJP (fully_fused_projection_bwd.cu:69-174) with the saved conic
@@ -369,7 +447,7 @@ template <int D> __global__ void scene_prim_bwd_kernel(SceneArgs a) {
             dL[r * D + c] = acc;
         }
     float gs[D], gl[NL];
-    const float *lt_raw = a.ltri + n * NL;
+    const float *lt_raw = rows.lt;
     const float R[9] = {1.f, lt_raw[0], lt_raw[1], -lt_raw[0], 1.f, lt_raw[2], -lt_raw[1],
                         -lt_raw[2], 1.f};
     float dR[9];
@@ -425,6 +503,7 @@ struct SceneWs {
     uint64_t *keys, *scratch;
     float4 *cols_n;
     float *grads; // v_m2 (2), v_cn (3), v_col (3), v_op, v_be per (view, primitive)
+    float *act;   // activated parameters (scene_act.cu)
     size_t bytes;
 };
 
@@ -452,6 +531,7 @@ SceneWs scene_ws(void *base, int32_t C, int64_t N, int32_t nb, int64_t cap) {
     w.scratch = reinterpret_cast<uint64_t *>(take(cap * 8));
     w.cols_n = reinterpret_cast<float4 *>(take((size_t)N * 16));
     w.grads = reinterpret_cast<float *>(take(CN * 10 * 4));
+    w.act = reinterpret_cast<float *>(take((size_t)N * kActPerPrim * 4));
     w.bytes = o;
     return w;
 }
@@ -522,6 +602,17 @@ int ubs_scene_workspace_offsets(int32_t C, int64_t N, int32_t n_buckets, int64_t
     return UBS_OK;
 }
 
+int ubs_scene_workspace_layout(int32_t C, int64_t N, int32_t n_buckets, int64_t capacity,
+                               int64_t *sections, int32_t n_sections) {
+    UBS_REQUIRE(sections && n_sections >= 0 && n_sections <= UBS_SCENE_WS_N_SECTIONS,
+                "scene_workspace_layout: bad section array (n=%d)", n_sections);
+    const SceneWs w = scene_ws(nullptr, C, N, n_buckets, capacity < 1 ? 1 : capacity);
+    const void *at[UBS_SCENE_WS_N_SECTIONS] = {w.recs, w.radius, w.depth, w.offsets, w.keys};
+    for (int i = 0; i < n_sections; ++i)
+        sections[i] = (int64_t)reinterpret_cast<uintptr_t>(at[i]);
+    return UBS_OK;
+}
+
 int ubs_scene_forward(int32_t dim, int64_t N, const float *xyz, const float *mean,
                       const float *scale, const float *l_triangle, const float *opacity,
                       const float *beta, const float *rgb, int32_t C, const float *viewmats,
@@ -584,9 +675,12 @@ int ubs_scene_forward_masked(int32_t dim, int64_t N, const float *xyz, const flo
     a.depth = w.depth;
     a.bucket_counts = w.bucket_counts;
     a.status = &w.hdr->status;
+    a.act = w.act;
     if (CN > 0) {
+        if (int e = launch_scene_act(N, dim, scale, beta, opacity, w.act, st)) return e;
         UBS_TIMED("scene_prim_fwd", st,
-                  UBS_SCENE_DIM(dim, scene_prim_fwd_kernel<DD><<<grid_for(CN, 128), 128, 0, st>>>(a)));
+                  UBS_SCENE_DIM(dim, scene_prim_fwd_kernel<DD><<<grid_for(CN, PRIM_THREADS),
+                                                                PRIM_THREADS, 0, st>>>(a)));
         note_launch();
         if (int e = check_launch("scene_prim_fwd")) return e;
     }
@@ -677,6 +771,7 @@ int ubs_scene_backward(int32_t dim, int64_t N, const float *xyz, const float *me
     a.radius = w.radius;
     a.depth = w.depth;
     a.status = &w.hdr->status;
+    a.act = w.act; // left by the forward
     a.v_m2 = v_m2;
     a.v_cn = v_cn;
     a.v_col = v_col;
@@ -691,7 +786,8 @@ int ubs_scene_backward(int32_t dim, int64_t N, const float *xyz, const float *me
     a.g_rgb = v_rgb;
     a.exact = exact_cond_grad;
     UBS_TIMED("scene_prim_bwd", st,
-              UBS_SCENE_DIM(dim, scene_prim_bwd_kernel<DD><<<grid_for(CN, 128), 128, 0, st>>>(a)));
+              UBS_SCENE_DIM(dim, scene_prim_bwd_kernel<DD><<<grid_for(CN, PRIM_THREADS),
+                                                                PRIM_THREADS, 0, st>>>(a)));
     note_launch();
     return check_launch("scene_prim_bwd");
 }

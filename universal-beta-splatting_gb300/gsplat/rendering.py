@@ -1,13 +1,20 @@
-"""rasterization(): the reference's pipeline entry point
-(submodules/gsplat/rendering.py:17-232) on the GB300 kernels.
+"""rasterization(): the entry point the Universal Beta Splatting model calls
+(submodules/gsplat/rendering.py:17-232), on the GB300 kernels.
 
-Same signature, outputs and `meta` keys.  Differences that do not change
-results: the covariance upper-triangle gather is fused into the projection
-kernel (same gradient), and the (camera, tile) offsets come out of the
-intersection count instead of a separate encode pass (same values).
+The call surface is the reference's: the same signature and argument
+checks, the same outputs and the same `meta` keys.  The body is organised
+around a render-mode table instead of branches: each mode names which
+per-primitive features are blended (the colours, the camera-space depth or
+both), whether the depth channel is divided by the alpha afterwards and
+whether the blended depth is turned into normals.  Everything else is one
+pass: projection (the upper-triangle gather of a 3x3 covariance happens
+inside the projection kernel), one intersection call that also yields the
+tile offsets, one blend.  The 32-channel chunking of wide feature rows
+lives in `rasterize_to_pixels` (channels blend independently, so the
+`channel_chunk` width does not change any result).
 """
 import math
-from typing import Dict, Optional, Tuple
+from typing import Dict, NamedTuple, Optional, Tuple
 
 import torch
 from torch import Tensor
@@ -16,7 +23,48 @@ from typing_extensions import Literal
 from .cuda._wrapper import _isect, fully_fused_projection, rasterize_to_pixels
 from .utils import depth_to_normal
 
-RENDER_MODES = ("RGB", "Normal", "Diffuse", "Specular", "Depth", "EDepth", "RGB+D", "RGB+ED")
+
+class _Mode(NamedTuple):
+    colors: bool           # blend the caller's colour channels
+    depth: bool            # blend the camera-space depth as one more channel
+    depth_over_alpha: bool  # divide that channel by the alpha afterwards
+    normals: bool          # turn the blended depth into world-space normals
+
+
+# Per render mode.  The reference divides by the alpha only when the mode
+# string contains "ED" *and* is tested against "ED"/"RGB+ED" -- "EDepth" is
+# not in that list (rendering.py:219), so "EDepth" returns the plain
+# accumulated depth; the table keeps that behaviour.
+_MODES: Dict[str, _Mode] = {
+    "RGB": _Mode(True, False, False, False),
+    "Diffuse": _Mode(True, False, False, False),
+    "Specular": _Mode(True, False, False, False),
+    "Depth": _Mode(False, True, False, False),
+    "EDepth": _Mode(False, True, False, False),
+    "Normal": _Mode(False, True, False, True),
+    "RGB+D": _Mode(True, True, False, False),
+    "RGB+ED": _Mode(True, True, True, False),
+}
+RENDER_MODES = tuple(_MODES)
+
+
+def _features(mode: _Mode, colors: Tensor, depths: Tensor, backgrounds: Optional[Tensor],
+              C: int) -> Tuple[Tensor, Optional[Tensor]]:
+    """Per-(camera, primitive) feature rows [C, N, F] and their backgrounds
+    [C, F] (None if the caller gave none) for one render mode.  The depth
+    channel's background is 0."""
+    rows, bgs = [], []
+    if mode.colors:
+        rows.append(colors if colors.dim() == 3 else colors.unsqueeze(0).expand(C, -1, -1))
+        bgs.append(backgrounds)
+    if mode.depth:
+        rows.append(depths.unsqueeze(-1))
+        if backgrounds is not None:
+            bgs.append(backgrounds.new_zeros(C, 1))
+    feats = rows[0] if len(rows) == 1 else torch.cat(rows, dim=-1)
+    if backgrounds is None:
+        return feats, None
+    return feats, (bgs[0] if len(bgs) == 1 else torch.cat(bgs, dim=-1))
 
 
 def rasterization(
@@ -43,9 +91,8 @@ def rasterization(
     channel_chunk: int = 32,
     covars: Optional[Tensor] = None,
 ) -> Tuple[Tensor, Tensor, Dict]:
-    meta = {}
-    N = means.shape[0]
-    C = viewmats.shape[0]
+    N, C = means.shape[0], viewmats.shape[0]
+    # the reference's argument checks (rendering.py:43-70)
     assert means.shape == (N, 3), means.shape
     if covars is None:
         assert l_triagnles.shape == (N, 4), l_triagnles.shape
@@ -57,85 +104,45 @@ def rasterization(
     assert betas.shape == (N,), betas.shape
     assert viewmats.shape == (C, 4, 4), viewmats.shape
     assert Ks.shape == (C, 3, 3), Ks.shape
-    assert render_mode in RENDER_MODES, render_mode
+    assert render_mode in _MODES, render_mode
     assert (colors.dim() == 2 and colors.shape[0] == N) or (
         colors.dim() == 3 and colors.shape[:2] == (C, N)
     ), colors.shape
+    assert channel_chunk > 0, channel_chunk
+    mode = _MODES[render_mode]
 
-    # the upper-triangle gather of the reference happens inside the kernel
-    radii, means2d, depths, conics, compensations = fully_fused_projection(
+    radii, means2d, depths, conics, comp = fully_fused_projection(
         means, covars, l_triagnles, scales, viewmats, Ks, width, height, eps2d=eps2d,
         near_plane=near_plane, far_plane=far_plane, radius_clip=radius_clip, sparse_grad=False,
-        calc_compensations=(rasterize_mode == "antialiased"), ortho=False)
-    opacities = opacities.repeat(C, 1)  # [C, N]
-    betas = betas.repeat(C, 1)  # [C, N]
-    camera_ids, primitive_ids = None, None
-    if compensations is not None:
-        opacities = opacities * compensations
-    meta.update({
-        "camera_ids": camera_ids,
-        "primitive_ids": primitive_ids,
-        "radii": radii,
-        "means2d": means2d,
-        "depths": depths,
-        "conics": conics,
-        "opacities": opacities,
-        "betas": betas,
-    })
+        calc_compensations=rasterize_mode == "antialiased", ortho=False)
+    # per-camera opacities (antialiased: scaled by the footprint compensation)
+    # and betas, [C, N]
+    opac_c = opacities.unsqueeze(0).expand(C, N)
+    if comp is not None:
+        opac_c = opac_c * comp
+    betas_c = betas.unsqueeze(0).expand(C, N)
 
-    if colors.dim() == 2:
-        colors = colors.expand(C, -1, -1)
-    if render_mode in ("RGB+D", "RGB+ED"):
-        colors = torch.cat((colors, depths[..., None]), dim=-1)
-        if backgrounds is not None:
-            backgrounds = torch.cat(
-                [backgrounds, torch.zeros(C, 1, device=backgrounds.device)], dim=-1)
-    elif render_mode in ("Depth", "EDepth", "Normal"):
-        colors = depths[..., None]
-        if backgrounds is not None:
-            backgrounds = torch.zeros(C, 1, device=backgrounds.device)
-
-    tile_width = math.ceil(width / float(tile_size))
-    tile_height = math.ceil(height / float(tile_size))
+    tiles_x = math.ceil(width / float(tile_size))
+    tiles_y = math.ceil(height / float(tile_size))
     tiles_per_gauss, isect_ids, flatten_ids, isect_offsets = _isect(
-        means2d.detach(), radii, depths.detach(), tile_size, tile_width, tile_height, sort=True)
-    meta.update({
-        "tile_width": tile_width,
-        "tile_height": tile_height,
-        "tiles_per_gauss": tiles_per_gauss,
-        "isect_ids": isect_ids,
-        "flatten_ids": flatten_ids,
-        "isect_offsets": isect_offsets,
-        "width": width,
-        "height": height,
-        "tile_size": tile_size,
-        "n_cameras": C,
-    })
+        means2d.detach(), radii, depths.detach(), tile_size, tiles_x, tiles_y, sort=True)
 
-    if colors.shape[-1] > channel_chunk:
-        n_chunks = (colors.shape[-1] + channel_chunk - 1) // channel_chunk
-        render_colors, render_alphas = [], []
-        for i in range(n_chunks):
-            cc = colors[..., i * channel_chunk:(i + 1) * channel_chunk]
-            bb = (backgrounds[..., i * channel_chunk:(i + 1) * channel_chunk]
-                  if backgrounds is not None else None)
-            rc, ra = rasterize_to_pixels(means2d, conics, cc, opacities, betas, width, height,
-                                         tile_size, isect_offsets, flatten_ids, backgrounds=bb)
-            render_colors.append(rc)
-            render_alphas.append(ra)
-        render_colors = torch.cat(render_colors, dim=-1)
-        render_alphas = render_alphas[0]
-    else:
-        render_colors, render_alphas = rasterize_to_pixels(
-            means2d, conics, colors, opacities, betas, width, height, tile_size, isect_offsets,
-            flatten_ids, backgrounds=backgrounds)
-    # the reference tests for the mode name "ED", so only "RGB+ED" is normalised
-    if render_mode in ("ED", "RGB+ED"):
-        render_colors = torch.cat(
-            [render_colors[..., :-1], render_colors[..., -1:] / render_alphas.clamp(min=1e-10)],
-            dim=-1)
-    if render_mode == "Normal":
-        camtoworlds = torch.inverse(viewmats)
-        render_colors = depth_to_normal(render_colors, camtoworlds, Ks)
-        render_colors = (render_colors + 1) / 2
-    return render_colors, render_alphas, meta
+    feats, feat_bg = _features(mode, colors, depths, backgrounds, C)
+    image, alpha = rasterize_to_pixels(means2d, conics, feats, opac_c, betas_c, width, height,
+                                       tile_size, isect_offsets, flatten_ids,
+                                       backgrounds=feat_bg)
+    if mode.depth_over_alpha:
+        image = torch.cat([image[..., :-1], image[..., -1:] / alpha.clamp(min=1e-10)], dim=-1)
+    if mode.normals:
+        image = (depth_to_normal(image, torch.inverse(viewmats), Ks) + 1) / 2
+
+    meta = {
+        "camera_ids": None, "primitive_ids": None,
+        "radii": radii, "means2d": means2d, "depths": depths, "conics": conics,
+        "opacities": opac_c, "betas": betas_c,
+        "tile_width": tiles_x, "tile_height": tiles_y,
+        "tiles_per_gauss": tiles_per_gauss, "isect_ids": isect_ids,
+        "flatten_ids": flatten_ids, "isect_offsets": isect_offsets,
+        "width": width, "height": height, "tile_size": tile_size, "n_cameras": C,
+    }
+    return image, alpha, meta

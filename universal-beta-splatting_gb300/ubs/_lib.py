@@ -63,6 +63,7 @@ SIGNATURES = {
                           + [_P] * 4 + [_I64, _P, _SZ, _P], _INT),
     "ubs_raster_pair_counts": ([_P, _P, _P], _INT),
     "ubs_scene_workspace_offsets": ([_I32, _I64, _I32, _I64, _I64P, _I64P], _INT),
+    "ubs_scene_workspace_layout": ([_I32, _I64, _I32, _I64, _I64P, _I32], _INT),
     "ubs_scene_forward_masked": ([_I32, _I64] + [_P] * 7 + [_I32] + [_P] * 7
                                  + [_I32, _I32, _F, _F, _F, _F] + [_P] * 4
                                  + [_I64, _P, _SZ, _P, _I32, _P], _INT),
@@ -98,6 +99,7 @@ SIGNATURES = {
                        _P, _SZ, _P], _INT),
     "ubs_fp32_probe_workspace_bytes": ([], _SZ),
     "ubs_fp32_probe": ([_I32, _P, _SZ, ctypes.POINTER(ctypes.c_double), _P], _INT),
+    "ubs_mufu_probe": ([_I32, _P, _SZ, ctypes.POINTER(ctypes.c_double), _P], _INT),
 }
 
 _lib = None

@@ -19,8 +19,18 @@ LIB_NAME = "libubs_gb300.so"
 LIB_PATH = os.path.join(BUILD, LIB_NAME)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "--use_fast_math", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-diag-suppress", "128"]
+# Every translation unit is built with fast math, as the reference's own CUDA
+# operators are (submodules/setup.py), except those that must round like
+# PyTorch's IEEE elementwise kernels (the parameter activations of the fused
+# render: scene_act.cu).
+FAST_MATH = ["--use_fast_math"]
+IEEE_SOURCES = ("scene_act.cu",)
+
+
+def _flags(src):
+    return NVCC_FLAGS + ([] if os.path.basename(src) in IEEE_SOURCES else FAST_MATH)
 
 
 def _nvcc():
@@ -43,7 +53,7 @@ def _fingerprint():
         h.update(f.encode())
         with open(f, "rb") as fh:
             h.update(fh.read())
-    h.update(" ".join(ARCH + NVCC_FLAGS).encode())
+    h.update(" ".join(ARCH + NVCC_FLAGS + FAST_MATH + list(IEEE_SOURCES)).encode())
     return h.hexdigest()
 
 
@@ -62,7 +72,7 @@ def build(force=False, verbose=False, jobs=None):
     for src in _sources():
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
-        cmds.append([nvcc] + ARCH + NVCC_FLAGS + ["-I", INCLUDE, "-c", src, "-o", obj])
+        cmds.append([nvcc] + ARCH + _flags(src) + ["-I", INCLUDE, "-c", src, "-o", obj])
 
     def run(cmd):
         if verbose:

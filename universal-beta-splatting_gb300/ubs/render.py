@@ -49,8 +49,14 @@ class Views:
             f[v, 0:16] = vm
             K = c.K.detach().float().cpu()
             f[v, 16:20] = torch.stack([K[0, 0], K[1, 1], K[0, 2], K[1, 2]])
-            if getattr(c, "position", None) is not None:
-                f[v, 20:23] = c.position.detach().reshape(3).float().cpu()
+            # the camera centre the reference model conditions on: the
+            # camera's own value (computed where its matrices live), so the
+            # view-direction queries round the same way
+            center = getattr(c, "position", None)
+            if center is None:
+                center = getattr(c, "center", None)
+            if center is not None:
+                f[v, 20:23] = center.detach().reshape(3).float().cpu()
             else:
                 R, t = vm.view(4, 4)[:3, :3], vm.view(4, 4)[:3, 3]
                 f[v, 20:23] = -R.t() @ t
@@ -167,6 +173,58 @@ class Renderer:
                ctypes.byref(r), ctypes.byref(d))
         n = views.C * N
         return self.last_ws[r.value:r.value + 4 * n].view(torch.int32).view(views.C, N)
+
+    def _sections(self, views: Views, N: int):
+        """Byte offsets of the last forward's workspace sections
+        (ubs_scene_workspace_layout: records, radii, depths, bucket starts,
+        keys)."""
+        secs = (ctypes.c_int64 * 5)()
+        L.call("ubs_scene_workspace_layout", views.C, N, views.n_buckets, self.last_cap, secs, 5)
+        return [int(x) for x in secs]
+
+    def projected(self, views: Views, N: int):
+        """The last forward's per-(view, primitive) projection, as the
+        reference's meta entries: dict of means2d [C, N, 2], conics [C, N, 3],
+        opacities [C, N] (conditioned), betas [C, N], radii int32 [C, N],
+        depths [C, N] (views into the workspace; zeros where the radius is 0)."""
+        rec, rad, dep, _, _ = self._sections(views, N)
+        n = views.C * N
+        r = self.last_ws[rec:rec + 32 * n].view(torch.float32).view(views.C, N, 8)
+        return {"means2d": r[..., 0:2], "opacities": r[..., 2], "betas": r[..., 3],
+                "conics": r[..., 4:7],
+                "radii": self.last_ws[rad:rad + 4 * n].view(torch.int32).view(views.C, N),
+                "depths": self.last_ws[dep:dep + 4 * n].view(torch.float32).view(views.C, N)}
+
+    def intersections(self, views: Views, N: int):
+        """The last forward's sorted intersections in the reference's layout,
+        one entry per view: (isect_ids int64 [T_v] = tile << 32 | depth bits,
+        flatten_ids int32 [T_v] = primitive index, isect_offsets int32
+        [th, tw]) -- what isect_tiles + isect_offset_encode return for that
+        view alone (isect_tiles.cu:82-96, 287-367).  Reads the intersection
+        count (synchronises)."""
+        T, _ = self.stats()
+        _, _, _, o_off, o_key = self._sections(views, N)
+        nb = views.n_buckets
+        # bucket starts (exclusive scan of the counts); the end of the last
+        # bucket is the intersection total
+        starts = self.last_ws[o_off:o_off + 4 * nb].view(torch.int32).long()
+        ends = torch.cat([starts[1:], starts.new_full((1,), T)])
+        keys = self.last_ws[o_key:o_key + 8 * T].view(torch.int64)
+        tb = views.tile_base.long().cpu()
+        out = []
+        for v in range(views.C):
+            b0, b1 = int(tb[v]), int(tb[v + 1])
+            a, b = int(starts[b0]), int(ends[b1 - 1])
+            k = keys[a:b]
+            counts = ends[b0:b1] - starts[b0:b1]
+            tile = torch.repeat_interleave(torch.arange(b1 - b0, device=k.device), counts)
+            ids = (tile << 32) | ((k >> 32) & 0xffffffff)
+            fl = ((k & 0xffffffff) - v * N).to(torch.int32)
+            h, w = views.shapes[v]
+            ts = views.tile_size
+            th, tw = (h + ts - 1) // ts, (w + ts - 1) // ts
+            out.append((ids, fl, (starts[b0:b1] - a).to(torch.int32).view(th, tw)))
+        return out
 
     def _args(self, p, views, bg):
         return [self.dim, p["xyz"].shape[0]] + [L.ptr(p[k]) for k in PARAM_ORDER] + [

@@ -61,6 +61,11 @@ class ServeConfig:
     max_batch_views: int = 8      # views per fused launch
     mem_budget: int = 16 << 30    # bytes of intersection buffers + images in flight
     margin: float = 1.25          # intersection estimate safety factor
+    # upper bound on a batch's estimated intersections (None: no bound): a
+    # batch's device time grows with its intersections, so under a latency
+    # target this keeps one large batch from holding its requests (and those
+    # queued behind it) past the target; the first request always goes
+    max_batch_isects: Optional[int] = None
     tile_size: int = 16
     keep_images: bool = False     # keep every image (tests); else only latency
 
@@ -92,7 +97,7 @@ class Scheduler:
     `cost(scene, cams, isects)` its device bytes.  Waiting requests are served
     first come first served: the oldest waiting request's scene forms the next
     batch, which takes that scene's waiting requests in arrival order up to
-    max_batch_views and the memory left."""
+    max_batch_views, max_batch_isects (estimated) and the memory left."""
 
     def __init__(self, cfg: ServeConfig, estimate: Callable, cost: Callable):
         self.cfg = cfg
@@ -115,7 +120,11 @@ class Scheduler:
             if r.scene != scene:
                 continue
             trial = cams + [r.camera]
-            cap = int(self.estimate(scene, trial) * self.cfg.margin) + 4096
+            est = self.estimate(scene, trial)
+            if chosen and self.cfg.max_batch_isects is not None and \
+                    est > self.cfg.max_batch_isects:
+                break
+            cap = int(est * self.cfg.margin) + 4096
             need = self.cost(scene, trial, cap)
             if chosen and self.in_flight_bytes + need > self.cfg.mem_budget:
                 break
