@@ -948,12 +948,16 @@ def run_config_d(dev, flush, rp):
     peak = torch.cuda.max_memory_allocated(dev)
     out = {"workload": "3M 6-D primitives, views 1920x1080 + 1600x1064 + 1280x720 + 960x540 "
                        "(fx = 1500 W/1920) in one fused forward + L1 + backward",
-           "tile_size": best, "autotune_ms": {str(k): round(v, 3) for k, v in
-                                              tuner.timings("configD").items()},
+           "tile_size": best, "blend_variant": {"forward": tuner.choice("configD")[1],
+                                                "backward": tuner.choice("configD")[2]},
+           "autotune_ms": {"tile %d / fwd variant %d / bwd variant %d" % k: round(v, 3)
+                           for k, v in tuner.timings("configD").items()},
            "ms_per_step": ms, "it_per_s": 1000.0 / ms, "isects": isects,
            "peak_memory_bytes": int(peak),
            "peak_memory_note": "torch.cuda.max_memory_allocated over the timed steps "
                                "(parameters, gradients, workspaces, images)"}
+    from ubs.autotune import set_blend_variant
+    set_blend_variant(0, 0)  # the later measurements use the default variant
     if rp is not None:
         r_ms = _ref_train_views(rp, p, cams, dev, 3, flush)
         out["ref_gpu_plain"] = {"ms_per_step": r_ms, "it_per_s": 1000.0 / r_ms,

@@ -420,7 +420,14 @@ int ubs_depth_colormap(const float *image, int64_t n_pixels, const float *table,
  *   - Nothing has to start at zero: each call clears the scratch's status
  *     header on `stream` itself.
  *   - One scratch per device: calls on the same device must not overlap in
- *     time (two streams, or unordered host threads, race on the records). */
+ *     time (two streams, or unordered host threads, race on the records).
+ *   - The scratch address is looked up once per device and kept for the life
+ *     of the process: after cudaDeviceReset on a device, do not call the
+ *     no-allocation entry points on that device again.
+ *   - Device-side status bits (8: a flatten index outside [0, C*N); 1: a
+ *     bounded wait ran out) go to the scratch's header; read them with
+ *     ubs_raster_noalloc_status (synchronises `stream`; the next call clears
+ *     them). */
 #define UBS_RASTER_NOALLOC_MAX_ISECTS 524288
 int ubs_raster_fwd_noalloc(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
                            const float *means2d, const float *conics, const float *colors,
@@ -429,6 +436,9 @@ int ubs_raster_fwd_noalloc(int32_t C, int64_t N, int32_t channels, int64_t n_ise
                            int32_t tile_width, int32_t tile_height, const int32_t *isect_offsets,
                            const int32_t *flatten_ids, float *render_colors, float *render_alphas,
                            int32_t *last_ids, void *stream);
+/* Status word of the last ubs_raster_fwd_noalloc on the current device (no
+ * reference counterpart): bits as ubs_raster_status; synchronises `stream`. */
+int ubs_raster_noalloc_status(uint32_t *status, void *stream);
 
 /* ------------------------------------------------------- fused multi-view ---
  * One render of a Universal Beta Splatting scene into C views at once (no
@@ -525,6 +535,22 @@ int ubs_scene_backward(int32_t dim, int64_t N, const float *xyz, const float *me
 /* Intersections counted by the last forward on `workspace` and its device
  * status word; synchronises the stream. */
 int ubs_scene_stats(const void *workspace, int64_t *n_isects, uint32_t *status, void *stream);
+
+/* Occupancy variant of the blend kernels (no reference counterpart; the
+ * reference's launch shape is fixed, rasterize_to_pixels_fwd.cu:269-292):
+ * for 3 channels and tiles of at most 16 x 16 pixels, each variant trades
+ * records per staged batch against CTAs per SM --
+ *   forward:  0 (default): 256-record batches, 8 CTAs per SM;
+ *             1: 128-record batches, 10 CTAs per SM; 2: 256-record, 6 CTAs per SM
+ *   backward: 0 (default): 128-record batches, 8 CTAs per SM;
+ *             1: 256-record batches, 6 CTAs per SM; 2: 128-record, 6 CTAs per SM
+ * (for 16 x 16 tiles; an 8 x 8 tile's batches are a quarter of that).
+ * Process-wide: it applies to every later launch from any thread (an
+ * autotuner sets it between measured steps, outside stream capture).  Images
+ * are identical under every variant; backward gradients agree up to the order
+ * of their atomic sums. */
+int ubs_set_blend_variant(int32_t forward, int32_t backward);
+int ubs_get_blend_variant(int32_t *forward, int32_t *backward);
 
 /* Device status word (bits: 1 wait timeout, 2 negative depth, 4 overflow,
  * 8 bad flatten index) and the contributing-pair count of the last packed

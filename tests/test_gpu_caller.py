@@ -56,7 +56,9 @@ def recorded(tag):
             if key.startswith(pre) and key != pre + "keywords":
                 v = FIX[key]
                 if v.dtype.kind in "fi" and v.ndim > 0:
-                    v = torch.from_numpy(v).to(DEV)
+                    # row-major copies: a transposed argument (the model passes
+                    # world_view_transform.transpose(0, 1)) is stored column-major
+                    v = torch.from_numpy(np.ascontiguousarray(v)).to(DEV)
                 else:
                     v = v.item()
                 args[key[len(pre):]] = v

@@ -208,6 +208,25 @@ def test_isect_long_buckets_and_empty(N):
     assert int(offs.abs().sum()) == 0
 
 
+@pytest.mark.parametrize("N,tie_every", [(65, 3), (129, 7), (1024, 4), (1025, 9), (300, 1)])
+def test_isect_bucket_sort_size_classes(N, tie_every):
+    """Buckets at the size-class edges of the per-bucket sort (65: the
+    smallest radix-sorted bucket, 129 and 1024: radix register blocks, 1025:
+    the first CTA-sorted size) with runs of equal depth every `tie_every`
+    keys (1: every key has the same depth, so every radix pass is skipped and
+    the tie pass sorts the whole bucket by index)."""
+    from gsplat.cuda._wrapper import isect_tiles
+    g = torch.Generator().manual_seed(N)
+    m2 = torch.rand(1, N, 2, generator=g) * 64
+    radii = torch.full((1, N), 100, dtype=torch.int32)
+    depths = torch.rand(1, N, generator=g) * 4 + 0.5
+    depths[0, ::tie_every] = 2.0
+    _, ids, fl = isect_tiles(m2.to(DEV), radii.to(DEV), depths.to(DEV), 16, 4, 4)
+    _, ids_o, fl_o = orc.isect_tiles(npy(m2), npy(radii), npy(depths), 16, 4, 4)
+    np.testing.assert_array_equal(npy(ids), ids_o)
+    np.testing.assert_array_equal(npy(fl), fl_o)
+
+
 def test_isect_rejects_negative_depth():
     from gsplat.cuda._wrapper import isect_tiles
     s = projected_scene(100, 64, 64, seed=3)

@@ -23,6 +23,7 @@
 //   * the backward sums the 7 + channels gradients of a record over a warp with
 //     transpose reductions (14 shuffles for 10 values), accumulates warps in
 //     shared memory and issues one global atomic per (tile, record, value).
+#include <atomic>
 #include <cstdio>
 
 #include "ubs_common.cuh"
@@ -256,7 +257,13 @@ __device__ __forceinline__ void gather_batch(const RasterArgs &a, GeoRec *srec, 
     for (int h = 0; h < RB; ++h) {
         const int s = tid + h * NT;
         if (s < cnt) {
-            const int64_t e = min(max((int64_t)ent[h], lo_e), hi_e);
+            // clamped for memory safety; a key outside the bucket's view
+            // (corrupt or stale) is reported like a bad flatten index
+            int64_t e = (int64_t)ent[h];
+            if (e < lo_e || e > hi_e) {
+                atomicOr(a.status, DEV_ERR_BAD_INDEX);
+                e = min(max(e, lo_e), hi_e);
+            }
             const char *src = reinterpret_cast<const char *>(a.entry_recs + e);
             char *dst = reinterpret_cast<char *>(srec + buf * BR + s);
             cp_async16(dst, src);
@@ -918,6 +925,17 @@ static int launch_pack(int64_t T, int64_t n_prims, const int32_t *fl, const floa
     return check_launch("pack_records");
 }
 
+// Occupancy variants of the 3-channel blend kernels for tiles of at most 128
+// threads (16 x 16 pixels and smaller), selected process-wide by
+// ubs_set_blend_variant: each trades records per staged batch (RB) against
+// CTAs per SM (MINB, the register bound it implies) --
+//   forward:  0: RB 2, 8 CTAs/SM;  1: RB 1, 10 CTAs/SM;  2: RB 2, 6 CTAs/SM
+//   backward: 0: RB 1, 8 CTAs/SM;  1: RB 2, 6 CTAs/SM;   2: RB 1, 6 CTAs/SM
+// Every variant computes the same images; the backward's gradient sums are
+// the same up to the order of their atomic additions.
+std::atomic<int> g_blend_fwd_variant{0}, g_blend_bwd_variant{0};
+constexpr int kBlendVariants = 3;
+
 template <int CD, bool BWD>
 static int launch_blend(RasterArgs &a, cudaStream_t st) {
     constexpr bool PACK = CD <= 4;
@@ -926,7 +944,11 @@ static int launch_blend(RasterArgs &a, cudaStream_t st) {
     // for the backward of 4 channels; wider colour rows need more registers),
     // the backward in batches of NT records to fit its shared memory.
     const bool small = PACK && NT <= 128;
-    const int RB = (small && BWD) ? 1 : 2;
+    const int variant = (small && CD == 3 && !a.pair_count)
+                            ? (BWD ? g_blend_bwd_variant.load() : g_blend_fwd_variant.load())
+                            : 0;
+    int RB = (small && BWD) ? 1 : 2;
+    if (variant == 1) RB = BWD ? 2 : 1;
     const SmemLayout L = smem_layout<CD, PACK, BWD>(NT, RB);
     if (L.total > 227 * 1024)
         return set_error(UBS_ERR_UNSUPPORTED, "raster: tile_size %d with %d channels needs %d B "
@@ -934,8 +956,14 @@ static int launch_blend(RasterArgs &a, cudaStream_t st) {
     const unsigned nblocks = (unsigned)a.n_buckets;
     if (nblocks == 0) return UBS_OK;
     void (*k)(RasterArgs) = nullptr;
+    if constexpr (CD == 3) {
+        if (small && variant == 1)
+            k = BWD ? raster_bwd_kernel<3, true, 2, 6> : raster_fwd_kernel<3, true, false, 1, 10>;
+        else if (small && variant == 2)
+            k = BWD ? raster_bwd_kernel<3, true, 1, 6> : raster_fwd_kernel<3, true, false, 2, 6>;
+    }
     if constexpr (PACK) {
-        if (small)
+        if (small && !k)
             k = BWD ? raster_bwd_kernel<CD, PACK, 1, (CD < 4 ? 8 : 7)>
                     : (a.pair_count ? raster_fwd_kernel<CD, PACK, true, 2, 8>
                                     : raster_fwd_kernel<CD, PACK, false, 2, 8>);
@@ -1205,6 +1233,23 @@ int ubs_raster_bwd(int32_t C, int64_t N, int32_t channels, int64_t n_isects,
                                  render_alphas, last_ids, v_render_colors, v_render_alphas,
                                  v_means2d, v_conics, v_colors, v_opacities, v_betas, 1,
                                  workspace, workspace_bytes, stream);
+}
+
+int ubs_set_blend_variant(int32_t forward, int32_t backward) {
+    UBS_REQUIRE(forward >= 0 && forward < kBlendVariants && backward >= 0 &&
+                    backward < kBlendVariants,
+                "set_blend_variant: variants %d, %d (supported 0 .. %d)", forward, backward,
+                kBlendVariants - 1);
+    g_blend_fwd_variant.store(forward);
+    g_blend_bwd_variant.store(backward);
+    return UBS_OK;
+}
+
+int ubs_get_blend_variant(int32_t *forward, int32_t *backward) {
+    UBS_REQUIRE(forward && backward, "get_blend_variant: null pointer");
+    *forward = g_blend_fwd_variant.load();
+    *backward = g_blend_bwd_variant.load();
+    return UBS_OK;
 }
 
 int ubs_raster_status(const void *workspace, uint32_t *status, uint64_t *pair_count,

@@ -22,6 +22,16 @@
 // There is one scratch per device, so calls on the same device must not
 // overlap: two calls in flight at once (different streams, or different host
 // threads without ordering between them) race on the records.
+//
+// The looked-up address is kept for the life of the process.  cudaDeviceReset
+// (or anything else that tears the device's primary context down) unloads the
+// library's device code, and the array may come back elsewhere: a process
+// that resets a device must not call the no-allocation entry points on it
+// again.
+//
+// Device-side status (a flatten index outside [0, C*N), a bounded wait that
+// ran out) lands in the scratch's header like it lands in a workspace's;
+// ubs_raster_noalloc_status reads it back.
 #include <atomic>
 #include <mutex>
 
@@ -86,6 +96,13 @@ int ubs_raster_fwd_noalloc(int32_t C, int64_t N, int32_t channels, int64_t n_ise
                           backgrounds, masks, width, height, tile_size, tile_width, tile_height,
                           isect_offsets, flatten_ids, render_colors, render_alphas, last_ids,
                           scratch, kScratchBytes, stream);
+}
+
+int ubs_raster_noalloc_status(uint32_t *status, void *stream) {
+    UBS_REQUIRE(status, "raster_noalloc_status: null pointer");
+    void *scratch = nullptr;
+    if (int e = scratch_for_current_device(&scratch)) return e;
+    return ubs_raster_status(scratch, status, nullptr, stream);
 }
 
 } // extern "C"

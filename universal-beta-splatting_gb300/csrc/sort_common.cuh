@@ -322,6 +322,21 @@ __device__ __forceinline__ void warp_sort_bucket(const uint64_t *__restrict__ ke
     }
 }
 
+// The lanes of `live` (which must all call this) whose 8-bit digit equals this
+// lane's: one vote per digit bit, each lane keeping the lanes that agree with
+// its own bit.  Eight votes replace a match instruction whose cost grows with
+// the number of distinct values in the warp.
+__device__ __forceinline__ uint32_t digit_peers(uint32_t d, uint32_t live) {
+    uint32_t peers = live;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        const bool set = (d >> b) & 1u;
+        const uint32_t votes = __ballot_sync(live, set);
+        peers &= set ? votes : ~votes;
+    }
+    return peers;
+}
+
 // Stable least-significant-digit radix sort of one bucket of n <= 32 E keys by
 // one warp, in shared memory `buf` (n keys) with a 256-bin histogram `hist`.
 // Keys are depth bits << 32 | entry index and unique within a bucket; the
@@ -332,7 +347,7 @@ __device__ __forceinline__ void warp_sort_bucket(const uint64_t *__restrict__ ke
 // such runs occur in training; they are short.  Element i of a pass is
 // lane i % 32 of round i / 32, so the rank of a key among equal digits is the
 // digit's running count plus the equal-digit lanes below it in its round
-// (match_any), which keeps every pass stable.
+// (digit_peers), which keeps every pass stable.
 template <int E>
 __device__ __forceinline__ void warp_radix_sort(uint64_t *buf, uint32_t *hist, int n, int lane) {
     uint64_t v[E];
@@ -342,18 +357,37 @@ __device__ __forceinline__ void warp_radix_sort(uint64_t *buf, uint32_t *hist, i
         v[r] = i < n ? buf[i] : 0ull;
     }
     const uint32_t lt = (1u << lane) - 1u;
+    // depth bits that differ somewhere in the bucket: a digit in which every
+    // key agrees would not move anything, so its pass is skipped
+    uint32_t all_and = 0xffffffffu, all_or = 0u;
+#pragma unroll
+    for (int r = 0; r < E; ++r)
+        if (r * 32 + lane < n) {
+            all_and &= (uint32_t)(v[r] >> 32);
+            all_or |= (uint32_t)(v[r] >> 32);
+        }
+    const uint32_t differ = __reduce_or_sync(0xffffffffu, all_or) &
+                            ~__reduce_and_sync(0xffffffffu, all_and);
 #pragma unroll 1
     for (int shift = 32; shift < 64; shift += 8) {
+        if (((differ >> (shift - 32)) & 255u) == 0u) continue;
 #pragma unroll
         for (int b = lane; b < 256; b += 32) hist[b] = 0u;
         __syncwarp();
+        // histogram: per round, the lowest lane of each group of equal digits
+        // adds the group's size (distinct digits, distinct bins: no atomics)
 #pragma unroll
-        for (int r = 0; r < E; ++r)
-            if (r * 32 + lane < n) atomicAdd(&hist[(uint32_t)(v[r] >> shift) & 255u], 1u);
-        __syncwarp();
-        // a digit that every key shares: this pass would not move anything
-        const uint32_t d0 = (uint32_t)(__shfl_sync(0xffffffffu, v[0], 0) >> shift) & 255u;
-        if (hist[d0] == (uint32_t)n) continue;
+        for (int r = 0; r < E; ++r) {
+            const int i = r * 32 + lane;
+            const uint32_t live = __ballot_sync(0xffffffffu, i < n);
+            if (live == 0u) break;
+            if (i < n) {
+                const uint32_t d = (uint32_t)(v[r] >> shift) & 255u;
+                const uint32_t peers = digit_peers(d, live);
+                if ((peers & lt) == 0u) hist[d] += __popc(peers);
+            }
+            __syncwarp();
+        }
         // exclusive scan of the 256 bins, 8 consecutive bins per lane
         uint32_t c[8], run = 0;
 #pragma unroll
@@ -371,6 +405,9 @@ __device__ __forceinline__ void warp_radix_sort(uint64_t *buf, uint32_t *hist, i
 #pragma unroll
         for (int k = 0; k < 8; ++k) hist[lane * 8 + k] = c[k] + inc - run;
         __syncwarp();
+        // scatter: a key's slot is its digit's running offset plus the equal
+        // digits of lower lanes in its round; the group's lowest lane then
+        // advances the offset
 #pragma unroll
         for (int r = 0; r < E; ++r) {
             const int i = r * 32 + lane;
@@ -378,11 +415,11 @@ __device__ __forceinline__ void warp_radix_sort(uint64_t *buf, uint32_t *hist, i
             if (live == 0u) break;
             if (i < n) {
                 const uint32_t d = (uint32_t)(v[r] >> shift) & 255u;
-                const uint32_t peers = __match_any_sync(live, d);
+                const uint32_t peers = digit_peers(d, live);
                 const uint32_t base = hist[d];
                 buf[base + __popc(peers & lt)] = v[r];
                 __syncwarp(live);
-                if ((peers & lt) == 0u) hist[d] = base + __popc(peers); // lowest peer
+                if ((peers & lt) == 0u) hist[d] = base + __popc(peers);
             }
             __syncwarp();
         }

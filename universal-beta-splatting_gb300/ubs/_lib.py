@@ -57,6 +57,9 @@ SIGNATURES = {
     "ubs_raster_fwd_noalloc": ([_I32, _I64, _I32, _I64] + [_P] * 7 + [_I32] * 5 + [_P] * 5 + [_P],
                                _INT),
     "ubs_raster_status": ([_P, _U32P, ctypes.POINTER(ctypes.c_uint64), _P], _INT),
+    "ubs_raster_noalloc_status": ([_U32P, _P], _INT),
+    "ubs_set_blend_variant": ([_I32, _I32], _INT),
+    "ubs_get_blend_variant": ([ctypes.POINTER(_I32), ctypes.POINTER(_I32)], _INT),
     "ubs_launch_count": ([], ctypes.c_ulonglong),
     "ubs_scene_workspace_bytes": ([_I32, _I64, _I32, _I64], _SZ),
     "ubs_scene_forward": ([_I32, _I64] + [_P] * 7 + [_I32] + [_P] * 7 + [_I32, _I32, _F, _F, _F, _F]
