@@ -966,7 +966,7 @@ def run_config_d(dev, flush, rp):
 
 
 SLO_MS = 10.0
-SERVED_RATES = (200, 300, 400, 500, 600, 700, 800, 1000)
+SERVED_RATES = (200, 300, 400, 450, 500, 550, 600, 650, 700, 800, 1000)
 PLAIN_RATES = (25, 50, 100, 150, 200, 300)
 
 
@@ -999,7 +999,7 @@ def run_serving(dev, rp, duration=3.0, rate=200.0, sweep_s=1.5):
     res = [(640, 480), (1280, 720), (1920, 1080)]
     # a batch's estimated intersections are bounded so that one batch's device
     # time stays a fraction of the latency target
-    cfg = ServeConfig(max_slots=4, max_batch_views=8, max_batch_isects=12_000_000)
+    cfg = ServeConfig(max_slots=4, max_batch_views=8, max_batch_isects=6_000_000)
     srv = Server(scenes, cfg)
     srv.calibrate({k: S.orbit_view(7, 4.0, 1280, 720, 1000.0, 1000.0, device=dev) for k in scenes})
     trace = poisson_trace(rate, duration, list(scenes), res, seed=0, device=dev)

@@ -210,11 +210,11 @@ def test_isect_long_buckets_and_empty(N):
 
 @pytest.mark.parametrize("N,tie_every", [(65, 3), (129, 7), (1024, 4), (1025, 9), (300, 1)])
 def test_isect_bucket_sort_size_classes(N, tie_every):
-    """Buckets at the size-class edges of the per-bucket sort (65: the
-    smallest radix-sorted bucket, 129 and 1024: radix register blocks, 1025:
-    the first CTA-sorted size) with runs of equal depth every `tie_every`
-    keys (1: every key has the same depth, so every radix pass is skipped and
-    the tie pass sorts the whole bucket by index)."""
+    """Buckets at the size-class edges of the per-bucket sort (65 and 129:
+    warp bitonic blocks of 2 and 4 keys per lane crossed, 1024: the largest
+    warp-sorted bucket, 1025: the first CTA-sorted size) with runs of equal
+    depth every `tie_every` keys (1: every key has the same depth, so the
+    order is the entry index alone)."""
     from gsplat.cuda._wrapper import isect_tiles
     g = torch.Generator().manual_seed(N)
     m2 = torch.rand(1, N, 2, generator=g) * 64

@@ -255,7 +255,8 @@ __device__ __forceinline__ M3 upper_sym(const float *oV) {
 
 constexpr int PRIM_THREADS = 128;
 
-template <int D> __global__ void __launch_bounds__(PRIM_THREADS) scene_prim_fwd_kernel(SceneArgs a) {
+template <int D>
+__global__ void __launch_bounds__(PRIM_THREADS, D == 6 ? 8 : 6) scene_prim_fwd_kernel(SceneArgs a) {
     __shared__ float stage[PRIM_THREADS / 32][stage_floats<D>()];
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
@@ -366,55 +367,36 @@ struct KeyWriter {
     }
 };
 
-// Where a primitive's raw-parameter gradients go: rows of the per-warp
-// gradient stage (one view: the warp then stores them coalesced), the
-// gradient tensors directly (one view, unstaged warps), or atomic adds into
-// the zeroed tensors (several views add into the same primitive).
-enum GradArray { G_XYZ, G_MEAN, G_SCALE, G_LTRI, G_OPAC, G_BETA, G_RGB, G_ARRAYS };
-
-template <int D> struct GradLayout {
-    static constexpr int K = D - 3, NL = D * (D - 1) / 2;
-    // floats per primitive of each gradient array, and their offsets in a
-    // stage of 32 primitives (one block of 32 rows per array)
-    static __host__ __device__ constexpr int width(int g) {
-        return g == G_XYZ ? 3 : g == G_MEAN ? K : g == G_SCALE ? D : g == G_LTRI ? NL
-               : g == G_OPAC ? 1 : g == G_BETA ? D - 2 : 3;
-    }
-    static __host__ __device__ constexpr int offset(int g) {
-        return g == 0 ? 0 : offset(g - 1) + 32 * width(g - 1);
-    }
-    static constexpr int floats = offset(G_ARRAYS);
-};
-
-template <int D> struct GradSink {
-    const SceneArgs *a;
-    float *stage; // this warp's gradient stage, or nullptr
-    int64_t n;
-    int lane;
-    bool direct;
-    __device__ __forceinline__ void operator()(int g, int k, float val) const {
-        using GL = GradLayout<D>;
-        if (stage) {
-            stage[GL::offset(g) + lane * GL::width(g) + k] = val;
-            return;
-        }
-        float *arr = g == G_XYZ ? a->g_xyz : g == G_MEAN ? a->g_mean : g == G_SCALE ? a->g_scale
-                     : g == G_LTRI ? a->g_ltri : g == G_OPAC ? a->g_opac : g == G_BETA ? a->g_beta
-                     : a->g_rgb;
-        float *p = arr + n * GL::width(g) + k;
-        if (direct) *p = val;
-        else if (val != 0.f) atomicAdd(p, val);
-    }
-};
-
-// Gradients of one rendered (view, primitive) entry with respect to its raw
-// parameters: the forward chain recomputed, then the projection, upper-
-// triangle gather, conditioning, covariance, rotation and activation VJPs.
-template <int D>
-__device__ __forceinline__ void prim_backward(const SceneArgs &a, const PrimRows &rows,
-                                              int64_t idx, int v, const GradSink<D> &out) {
+template <int D> __global__ void __launch_bounds__(PRIM_THREADS) scene_prim_bwd_kernel(SceneArgs a) {
     constexpr int K = D - 3;
     constexpr int NL = D * (D - 1) / 2;
+    __shared__ float stage[PRIM_THREADS / 32][stage_floats<D>()];
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int v = (int)(idx / a.N);
+    const int64_t n = idx - (int64_t)v * a.N;
+    PrimRows rows;
+    if (prim_rows<D>(a, idx, n, lane, stage[threadIdx.x >> 5], rows)) __syncwarp();
+    if (idx >= (int64_t)a.C * a.N) return;
+    const bool direct = a.C == 1; // one view: plain stores, else atomics into zeroed grads
+    if (a.radius[idx] <= 0) {
+        if (direct) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) a.g_xyz[n * 3 + k] = 0.f;
+#pragma unroll
+            for (int k = 0; k < K; ++k) a.g_mean[n * K + k] = 0.f;
+#pragma unroll
+            for (int k = 0; k < D; ++k) a.g_scale[n * D + k] = 0.f;
+#pragma unroll
+            for (int k = 0; k < NL; ++k) a.g_ltri[n * NL + k] = 0.f;
+            a.g_opac[n] = 0.f;
+#pragma unroll
+            for (int k = 0; k < D - 2; ++k) a.g_beta[n * (D - 2) + k] = 0.f;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) a.g_rgb[n * 3 + k] = 0.f;
+        }
+        return;
+    }
     PrimFwd<D> f;
     prim_forward<D>(a, rows, v, f);
     const Cam cam = view_cam(a, v);
@@ -489,65 +471,25 @@ __device__ __forceinline__ void prim_backward(const SceneArgs &a, const PrimRows
     for (int r = 3; r < D; ++r)
 #pragma unroll
         for (int c = 0; c < r; ++c) gl[m++] = dL[r * D + c];
-    // activation VJPs
+    // activation VJPs and stores
+    auto put = [&](float *p, float val) {
+        if (direct) *p = val;
+        else if (val != 0.f) atomicAdd(p, val);
+    };
 #pragma unroll
-    for (int k = 0; k < 3; ++k) out(G_XYZ, k, gm[k]);
+    for (int k = 0; k < 3; ++k) put(&a.g_xyz[n * 3 + k], gm[k]);
 #pragma unroll
-    for (int k = 0; k < K; ++k) out(G_MEAN, k, gm[3 + k]);
+    for (int k = 0; k < K; ++k) put(&a.g_mean[n * K + k], gm[3 + k]);
 #pragma unroll
-    for (int k = 0; k < D; ++k) out(G_SCALE, k, gs[k] * sigmoid_f(a.scale[out.n * D + k]));
+    for (int k = 0; k < D; ++k) put(&a.g_scale[n * D + k], gs[k] * sigmoid_f(a.scale[n * D + k]));
 #pragma unroll
-    for (int k = 0; k < NL; ++k) out(G_LTRI, k, gl[k]);
-    out(G_OPAC, 0, go * f.o * (1.f - f.o));
-    out(G_BETA, 0, a.v_be[idx] * f.b0);
+    for (int k = 0; k < NL; ++k) put(&a.g_ltri[n * NL + k], gl[k]);
+    put(&a.g_opac[n], go * f.o * (1.f - f.o));
+    put(&a.g_beta[n * (D - 2)], a.v_be[idx] * f.b0);
 #pragma unroll
-    for (int k = 0; k < K; ++k) out(G_BETA, 1 + k, gb[k] * f.b[k]);
+    for (int k = 0; k < K; ++k) put(&a.g_beta[n * (D - 2) + 1 + k], gb[k] * f.b[k]);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) out(G_RGB, k, a.v_col[idx * 3 + k]);
-}
-
-template <int D>
-__global__ void __launch_bounds__(PRIM_THREADS, D == 6 ? 4 : 3) scene_prim_bwd_kernel(SceneArgs a) {
-    using GL = GradLayout<D>;
-    __shared__ float stage[PRIM_THREADS / 32][stage_floats<D>()];
-    __shared__ float gstage[PRIM_THREADS / 32][GL::floats];
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int v = (int)(idx / a.N);
-    const int64_t n = idx - (int64_t)v * a.N;
-    PrimRows rows;
-    const bool staged = prim_rows<D>(a, idx, n, lane, stage[wid], rows);
-    if (staged) __syncwarp();
-    if (idx >= (int64_t)a.C * a.N) return; // (lanes of unstaged warps only)
-    GradSink<D> out;
-    out.a = &a;
-    out.n = n;
-    out.lane = lane;
-    out.direct = a.C == 1; // one view: plain stores, else atomics into zeroed grads
-    // one view and a staged warp: gradient rows through the stage, stored
-    // coalesced by the whole warp
-    out.stage = (out.direct && staged) ? gstage[wid] : nullptr;
-    const bool live = a.radius[idx] > 0;
-    if (live) {
-        prim_backward<D>(a, rows, idx, v, out);
-    } else if (out.direct) {
-#pragma unroll
-        for (int g = 0; g < G_ARRAYS; ++g)
-            for (int k = 0; k < GL::width(g); ++k) out(g, k, 0.f);
-    }
-    if (!out.stage) return;
-    __syncwarp();
-    const int64_t n0 = n - lane;
-    float *const arrs[G_ARRAYS] = {a.g_xyz, a.g_mean, a.g_scale, a.g_ltri, a.g_opac, a.g_beta,
-                                   a.g_rgb};
-#pragma unroll
-    for (int g = 0; g < G_ARRAYS; ++g) {
-        const int w = GL::width(g);
-        float *dst = arrs[g] + n0 * w;
-        const float *src = gstage[wid] + GL::offset(g);
-#pragma unroll
-        for (int j = 0; j < w; ++j) dst[j * 32 + lane] = src[j * 32 + lane];
-    }
+    for (int k = 0; k < 3; ++k) put(&a.g_rgb[n * 3 + k], a.v_col[idx * 3 + k]);
 }
 
 size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -743,9 +685,19 @@ int ubs_scene_forward_masked(int32_t dim, int64_t N, const float *xyz, const flo
         note_launch();
         if (int e = check_launch("scene_prim_fwd")) return e;
     }
-    if (int e = device_exclusive_scan<int32_t>(w.bucket_counts, w.offsets, n_buckets,
-                                               w.block_sums, &w.hdr->total, st))
+    // bucket offsets, total and heaviest-first order: one CTA when the
+    // buckets fit it, else a device-wide scan and the order kernel below
+    const bool one_cta = n_buckets <= SCAN_ORDER_MAX;
+    if (one_cta) {
+        UBS_TIMED("bucket_scan_order", st,
+                  bucket_scan_order_kernel<<<1, 1024, 0, st>>>(w.bucket_counts, n_buckets,
+                                                               w.offsets, &w.hdr->total, w.order));
+        note_launch();
+        if (int e = check_launch("bucket_scan_order")) return e;
+    } else if (int e = device_exclusive_scan<int32_t>(w.bucket_counts, w.offsets, n_buckets,
+                                                      w.block_sums, &w.hdr->total, st)) {
         return e;
+    }
     if (cudaMemcpyAsync(w.cursor, w.offsets, (size_t)n_buckets * 4, cudaMemcpyDeviceToDevice, st) !=
         cudaSuccess)
         return check_launch("scene cursor copy");
@@ -761,11 +713,13 @@ int ubs_scene_forward_masked(int32_t dim, int64_t N, const float *xyz, const flo
     if (int e = launch_bucket_sort(n_buckets, w.offsets, &w.hdr->total, capacity, w.keys,
                                    w.scratch, w.big_list, &w.hdr->n_big, wr, st))
         return e;
-    UBS_TIMED("bucket_order", st,
-              bucket_order_kernel<<<1, 1024, 0, st>>>(w.offsets, &w.hdr->total, capacity,
-                                                      n_buckets, w.order));
-    note_launch();
-    if (int e = check_launch("bucket_order")) return e;
+    if (!one_cta) {
+        UBS_TIMED("bucket_order", st,
+                  bucket_order_kernel<<<1, 1024, 0, st>>>(w.offsets, &w.hdr->total, capacity,
+                                                          n_buckets, w.order));
+        note_launch();
+        if (int e = check_launch("bucket_order")) return e;
+    }
     return scene_blend(1, C, CN, n_buckets, tile_size, w.offsets, w.order, &w.hdr->total, capacity,
                        w.keys, w.recs, w.cols_n, backgrounds, tile_base, view_dims, pix_base,
                        render_colors, render_alphas, last_ids, nullptr, nullptr, nullptr, nullptr,

@@ -256,6 +256,84 @@ static __global__ void __launch_bounds__(1024) bucket_order_kernel(const int32_t
     for (int32_t b = tid; b < n_buckets; b += blockDim.x) order[atomicAdd(&bins[bin_of(b)], 1)] = b;
 }
 
+// Both per-bucket passes of a frame whose buckets fit one CTA (n <=
+// SCAN_ORDER_MAX), in one launch: the exclusive scan of the bucket counts
+// (bucket offsets, int32, and the intersection total) and the heaviest-first
+// bucket order of bucket_order_kernel (a counting sort by record count).
+// Each of the 1024 threads scans a contiguous run of buckets.
+constexpr int SCAN_ORDER_MAX = 1024 * 64;
+static __global__ void __launch_bounds__(1024) bucket_scan_order_kernel(
+    const int32_t *__restrict__ counts, int32_t n, int32_t *__restrict__ offsets,
+    int64_t *__restrict__ total, int32_t *__restrict__ order) {
+    __shared__ int32_t bins[ORDER_BINS];
+    __shared__ int64_t wtot[32];
+    __shared__ int32_t btot[32];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int per = (n + 1023) / 1024;
+    const int b0 = min(n, tid * per), b1 = min(n, b0 + per);
+    for (int i = tid; i < ORDER_BINS; i += blockDim.x) bins[i] = 0;
+    __syncthreads();
+    int64_t run = 0;
+    for (int b = b0; b < b1; ++b) {
+        const int32_t c = counts[b];
+        run += c;
+        const int64_t q = c >> 2;
+        atomicAdd(&bins[ORDER_BINS - 1 - (int)(q < ORDER_BINS - 1 ? q : ORDER_BINS - 1)], 1);
+    }
+    int64_t inc = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int64_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) wtot[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        const int64_t w = wtot[lane];
+        int64_t wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += y;
+        }
+        wtot[lane] = wi - w; // exclusive
+    }
+    __syncthreads();
+    int64_t off = wtot[wid] + inc - run;
+    for (int b = b0; b < b1; ++b) {
+        offsets[b] = (int32_t)off;
+        off += counts[b];
+    }
+    if (tid == blockDim.x - 1) *total = off;
+    // heaviest-first order: exclusive scan of the bins, then a scatter
+    const int v = bins[tid];
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) btot[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int t = btot[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        btot[lane] = t; // inclusive
+    }
+    __syncthreads();
+    bins[tid] = x - v + (wid ? btot[wid - 1] : 0);
+    __syncthreads();
+    for (int b = b0; b < b1; ++b) {
+        const int64_t q = counts[b] >> 2;
+        order[atomicAdd(&bins[ORDER_BINS - 1 - (int)(q < ORDER_BINS - 1 ? q : ORDER_BINS - 1)],
+                        1)] = b;
+    }
+}
+
 // Bitonic sort of the 32 * E keys of a warp held E per lane in registers,
 // blocked (element i = lane * E + e): exchange distances below E stay inside
 // a lane, larger ones are lane-xor shuffles.  Only the loop over a lane's E
@@ -322,174 +400,16 @@ __device__ __forceinline__ void warp_sort_bucket(const uint64_t *__restrict__ ke
     }
 }
 
-// The lanes of `live` (which must all call this) whose 8-bit digit equals this
-// lane's: one vote per digit bit, each lane keeping the lanes that agree with
-// its own bit.  Eight votes replace a match instruction whose cost grows with
-// the number of distinct values in the warp.
-__device__ __forceinline__ uint32_t digit_peers(uint32_t d, uint32_t live) {
-    uint32_t peers = live;
-#pragma unroll
-    for (int b = 0; b < 8; ++b) {
-        const bool set = (d >> b) & 1u;
-        const uint32_t votes = __ballot_sync(live, set);
-        peers &= set ? votes : ~votes;
-    }
-    return peers;
-}
-
-// Stable least-significant-digit radix sort of one bucket of n <= 32 E keys by
-// one warp, in shared memory `buf` (n keys) with a 256-bin histogram `hist`.
-// Keys are depth bits << 32 | entry index and unique within a bucket; the
-// passes order them by the 32 depth bits (four 8-bit digits; a pass whose
-// digit is the same for every key is skipped), which leaves equal depths in
-// their emit order, and a last step sorts each run of equal depths by the
-// whole key (its entry index).  Relocated primitives are exact copies, so
-// such runs occur in training; they are short.  Element i of a pass is
-// lane i % 32 of round i / 32, so the rank of a key among equal digits is the
-// digit's running count plus the equal-digit lanes below it in its round
-// (digit_peers), which keeps every pass stable.
-template <int E>
-__device__ __forceinline__ void warp_radix_sort(uint64_t *buf, uint32_t *hist, int n, int lane) {
-    uint64_t v[E];
-#pragma unroll
-    for (int r = 0; r < E; ++r) {
-        const int i = r * 32 + lane;
-        v[r] = i < n ? buf[i] : 0ull;
-    }
-    const uint32_t lt = (1u << lane) - 1u;
-    // depth bits that differ somewhere in the bucket: a digit in which every
-    // key agrees would not move anything, so its pass is skipped
-    uint32_t all_and = 0xffffffffu, all_or = 0u;
-#pragma unroll
-    for (int r = 0; r < E; ++r)
-        if (r * 32 + lane < n) {
-            all_and &= (uint32_t)(v[r] >> 32);
-            all_or |= (uint32_t)(v[r] >> 32);
-        }
-    const uint32_t differ = __reduce_or_sync(0xffffffffu, all_or) &
-                            ~__reduce_and_sync(0xffffffffu, all_and);
-#pragma unroll 1
-    for (int shift = 32; shift < 64; shift += 8) {
-        if (((differ >> (shift - 32)) & 255u) == 0u) continue;
-#pragma unroll
-        for (int b = lane; b < 256; b += 32) hist[b] = 0u;
-        __syncwarp();
-        // histogram: per round, the lowest lane of each group of equal digits
-        // adds the group's size (distinct digits, distinct bins: no atomics)
-#pragma unroll
-        for (int r = 0; r < E; ++r) {
-            const int i = r * 32 + lane;
-            const uint32_t live = __ballot_sync(0xffffffffu, i < n);
-            if (live == 0u) break;
-            if (i < n) {
-                const uint32_t d = (uint32_t)(v[r] >> shift) & 255u;
-                const uint32_t peers = digit_peers(d, live);
-                if ((peers & lt) == 0u) hist[d] += __popc(peers);
-            }
-            __syncwarp();
-        }
-        // exclusive scan of the 256 bins, 8 consecutive bins per lane
-        uint32_t c[8], run = 0;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            c[k] = run;
-            run += hist[lane * 8 + k];
-        }
-        uint32_t inc = run;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
-            if (lane >= o) inc += y;
-        }
-        __syncwarp();
-#pragma unroll
-        for (int k = 0; k < 8; ++k) hist[lane * 8 + k] = c[k] + inc - run;
-        __syncwarp();
-        // scatter: a key's slot is its digit's running offset plus the equal
-        // digits of lower lanes in its round; the group's lowest lane then
-        // advances the offset
-#pragma unroll
-        for (int r = 0; r < E; ++r) {
-            const int i = r * 32 + lane;
-            const uint32_t live = __ballot_sync(0xffffffffu, i < n);
-            if (live == 0u) break;
-            if (i < n) {
-                const uint32_t d = (uint32_t)(v[r] >> shift) & 255u;
-                const uint32_t peers = digit_peers(d, live);
-                const uint32_t base = hist[d];
-                buf[base + __popc(peers & lt)] = v[r];
-                __syncwarp(live);
-                if ((peers & lt) == 0u) hist[d] = base + __popc(peers);
-            }
-            __syncwarp();
-        }
-#pragma unroll
-        for (int r = 0; r < E; ++r) {
-            const int i = r * 32 + lane;
-            if (i < n) v[r] = buf[i];
-        }
-        __syncwarp();
-    }
-    // buf holds the keys in v's order (the last pass that moved anything left
-    // them there; with no such pass they never left).  Runs of equal depth:
-    // the lane holding a run's first key sorts the run by the whole key
-    // (insertion sort; runs are short and disjoint, and other lanes only read
-    // a run's depth words, which the sort does not change)
-    bool tie = false;
-#pragma unroll
-    for (int r = 0; r < E; ++r) {
-        const int i = r * 32 + lane;
-        if (i + 1 < n && (uint32_t)(v[r] >> 32) == (uint32_t)(buf[i + 1] >> 32)) tie = true;
-    }
-    if (!__any_sync(0xffffffffu, tie)) return;
-#pragma unroll
-    for (int r = 0; r < E; ++r) {
-        const int i = r * 32 + lane;
-        if (i >= n) continue;
-        const uint32_t hi = (uint32_t)(v[r] >> 32);
-        const bool starts = (i == 0 || (uint32_t)(buf[i - 1] >> 32) != hi);
-        if (!starts || i + 1 >= n || (uint32_t)(buf[i + 1] >> 32) != hi) continue;
-        int end = i + 1;
-        while (end < n && (uint32_t)(buf[end] >> 32) == hi) ++end;
-        for (int a = i + 1; a < end; ++a) {
-            const uint64_t key = buf[a];
-            int b = a - 1;
-            while (b >= i && buf[b] > key) {
-                buf[b + 1] = buf[b];
-                --b;
-            }
-            buf[b + 1] = key;
-        }
-    }
-    __syncwarp();
-}
-
-constexpr int RADIX_MIN = 64;  // buckets longer than this use the warp radix sort
-constexpr int SORT_WARPS = 4;  // warps (buckets) per CTA of the warp-level sort
-
-template <int E, typename Writer>
-__device__ __forceinline__ void warp_radix_bucket(const uint64_t *__restrict__ keys, int64_t lo,
-                                                  int n, int64_t bkt, int lane, uint64_t *buf,
-                                                  uint32_t *hist, const Writer &w) {
-    for (int i = lane; i < n; i += 32) buf[i] = keys[lo + i];
-    __syncwarp();
-    warp_radix_sort<E>(buf, hist, n, lane);
-    for (int i = lane; i < n; i += 32) w(buf[i], lo + i, bkt);
-}
-
-// One warp per bucket for buckets of at most WARP_SEG keys: up to RADIX_MIN
-// keys a bitonic network in registers (padded to a power of two >= 32 with
-// all-ones keys, which sort last), longer ones the radix sort above; longer
+// One warp per bucket for buckets of at most WARP_SEG keys (padded to the
+// next power of two >= 32 with all-ones keys, which sort last); longer
 // buckets go to the device-side lists: mid (<= SMALL_SEG) from the front of
 // `lists`, big from the back.  counters = {n_big, n_mid}.
 template <typename Writer>
-__global__ void __launch_bounds__(SORT_WARPS * 32) bucket_sort_warp_kernel(
+__global__ void __launch_bounds__(256) bucket_sort_warp_kernel(
     int64_t n_buckets, const int32_t *__restrict__ offsets, const int64_t *T_dev, int64_t cap,
     const uint64_t *__restrict__ keys, int32_t *lists, int32_t *counters, Writer w) {
-    __shared__ uint64_t sbuf[SORT_WARPS][WARP_SEG];
-    __shared__ uint32_t shist[SORT_WARPS][256];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int64_t bkt = (int64_t)blockIdx.x * SORT_WARPS + wid;
+    const int lane = threadIdx.x & 31;
+    const int64_t bkt = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
     if (bkt >= n_buckets) return;
     const int64_t T = T_dev ? imin64(*T_dev, cap) : cap;
     int64_t lo, hi;
@@ -504,14 +424,12 @@ __global__ void __launch_bounds__(SORT_WARPS * 32) bucket_sort_warp_kernel(
         return;
     }
     const int m = (int)n;
-    uint64_t *buf = sbuf[wid];
-    uint32_t *hist = shist[wid];
     if (m <= 32) warp_sort_bucket<1>(keys, lo, m, bkt, lane, w);
-    else if (m <= RADIX_MIN) warp_sort_bucket<2>(keys, lo, m, bkt, lane, w);
-    else if (m <= 128) warp_radix_bucket<4>(keys, lo, m, bkt, lane, buf, hist, w);
-    else if (m <= 256) warp_radix_bucket<8>(keys, lo, m, bkt, lane, buf, hist, w);
-    else if (m <= 512) warp_radix_bucket<16>(keys, lo, m, bkt, lane, buf, hist, w);
-    else warp_radix_bucket<32>(keys, lo, m, bkt, lane, buf, hist, w);
+    else if (m <= 64) warp_sort_bucket<2>(keys, lo, m, bkt, lane, w);
+    else if (m <= 128) warp_sort_bucket<4>(keys, lo, m, bkt, lane, w);
+    else if (m <= 256) warp_sort_bucket<8>(keys, lo, m, bkt, lane, w);
+    else if (m <= 512) warp_sort_bucket<16>(keys, lo, m, bkt, lane, w);
+    else warp_sort_bucket<32>(keys, lo, m, bkt, lane, w);
 }
 
 // Buckets of WARP_SEG < n <= SMALL_SEG keys (the mid list): a fixed grid walks
@@ -613,8 +531,7 @@ inline int launch_bucket_sort(int64_t n_buckets, const int32_t *offsets, const i
     if (n_buckets <= 0 || cap <= 0) return UBS_OK;
     if (cudaMemsetAsync(counters, 0, 8, st) != cudaSuccess) return check_launch("sort memset");
     UBS_TIMED("bucket_sort_warp", st,
-              bucket_sort_warp_kernel<Writer><<<grid_for(n_buckets, SORT_WARPS),
-                                               SORT_WARPS * 32, 0, st>>>(
+              bucket_sort_warp_kernel<Writer><<<grid_for(n_buckets, 8), 256, 0, st>>>(
                   n_buckets, offsets, T_dev, cap, keys, lists, counters, w));
     note_launch();
     if (cap > WARP_SEG) {
