@@ -203,7 +203,7 @@ def test_kernel_timer_eager_and_graph_replays():
     colors, alphas = Renderer(dim=6).render(leaves, views)
     (colors.sum() + alphas.sum()).backward()
     k = L.profile_stop()
-    for name in ("scene_prim_fwd", "scene_emit", "bucket_sort_warp", "bucket_order", "raster_fwd",
+    for name in ("scene_prim_fwd", "scene_emit", "bucket_sort_warp", "bucket_scan_order", "raster_fwd",
                  "raster_bwd", "scene_prim_bwd"):
         assert name in k and k[name][0] >= 1 and k[name][1] > 0, (name, k.get(name))
     # fresh leaves: these went through an eager backward on the default stream

@@ -182,8 +182,8 @@ __device__ __forceinline__ void warp_emit_rects(uint32_t n, uint32_t bw, uint32_
         if (lane >= o) incl += y;
     }
     const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    for (uint32_t base = 0; base < total; base += 32) {
-        const uint32_t j = base + lane;
+    // pair j of the flattened list: the cursor of its tile and its entry's key
+    auto locate = [&](uint32_t j, int32_t *&slot, uint64_t &k) {
         int owner = 0; // first lane whose inclusive count exceeds j
 #pragma unroll
         for (int step = 16; step > 0; step >>= 1) {
@@ -194,14 +194,30 @@ __device__ __forceinline__ void warp_emit_rects(uint32_t n, uint32_t bw, uint32_
         const uint32_t o_n = __shfl_sync(0xffffffffu, n, owner);
         const uint32_t o_bw = __shfl_sync(0xffffffffu, bw, owner);
         const uint32_t o_pitch = __shfl_sync(0xffffffffu, pitch, owner);
-        const uint64_t o_key = __shfl_sync(0xffffffffu, key, owner);
+        k = __shfl_sync(0xffffffffu, key, owner);
         int32_t *o_cur = reinterpret_cast<int32_t *>(
             __shfl_sync(0xffffffffu, reinterpret_cast<uintptr_t>(cur), owner));
-        if (j < total) {
-            const uint32_t local = j - (o_incl - o_n);
-            const uint32_t ry = local / o_bw, rx = local - ry * o_bw;
-            const int32_t pos = atomicAdd(o_cur + (int64_t)ry * o_pitch + rx, 1);
-            if (pos >= 0 && pos < cap) keys[pos] = o_key;
+        const uint32_t local = j - (o_incl - o_n);
+        const uint32_t ry = local / o_bw, rx = local - ry * o_bw;
+        slot = o_cur + (int64_t)ry * o_pitch + rx;
+    };
+    // two rounds per iteration: both rounds' cursor atomics are in flight
+    // before either round stores its keys
+    for (uint32_t base = 0; base < total; base += 64) {
+        const uint32_t j0 = base + lane, j1 = base + 32 + lane;
+        int32_t *s0, *s1;
+        uint64_t k0, k1;
+        locate(j0, s0, k0);
+        const bool two = base + 32 < total; // warp-uniform
+        if (two) locate(j1, s1, k1);
+        const int32_t p0 = j0 < total ? atomicAdd(s0, 1) : -1;
+        const int32_t p1 = (two && j1 < total) ? atomicAdd(s1, 1) : -1;
+        if (j0 < total) {
+            if (p0 >= 0 && p0 < cap) keys[p0] = k0;
+            else atomicOr(status, DEV_ERR_OVERFLOW);
+        }
+        if (two && j1 < total) {
+            if (p1 >= 0 && p1 < cap) keys[p1] = k1;
             else atomicOr(status, DEV_ERR_OVERFLOW);
         }
     }
