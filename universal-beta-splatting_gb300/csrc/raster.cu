@@ -171,12 +171,11 @@ struct SmemLayout {
 template <int CD, bool PACK, bool BWD>
 __host__ __device__ inline SmemLayout smem_layout(int NT, int RB = 2) {
     constexpr int NV = 7 + CD; // gradient values per record
-    // one culling mask per half-warp (8 x 4 pixels): 2 nw targets
     const int nw = NT / 32, BR = RB * NT;
     SmemLayout L;
     L.mask_off = 16; // after two mbarriers
-    // per-target masks (2 nw x RB nw words), then one int per target
-    L.rec_off = (L.mask_off + 2 * nw * RB * nw * 4 + 2 * nw * 4 + 127) & ~127;
+    // per-target-warp masks (nw x RB nw words), then one int per warp
+    L.rec_off = (L.mask_off + nw * RB * nw * 4 + nw * 4 + 127) & ~127;
     const int colbytes = PACK ? 16 : CD * 4;
     L.col_off = L.rec_off + 2 * BR * (int)sizeof(GeoRec);
     L.gacc_off = (L.col_off + 2 * BR * colbytes + 15) & ~15;
@@ -199,17 +198,16 @@ __device__ __forceinline__ bool conic_pd(const GeoRec &r) {
     const float det = r.cxx * r.cyy - r.cxy * r.cxy;
     return (r.cxx > 0.f) && (r.cyy > 0.f) && (det > 1e-3f * r.cxx * r.cyy);
 }
-__device__ __forceinline__ bool ellipse_hits_box(const GeoRec &r, bool pd, float bx0, float by0,
-                                                 float bh = 7.f) {
+__device__ __forceinline__ bool ellipse_hits_box(const GeoRec &r, bool pd, float bx0, float by0) {
     if (!pd) return true;
     const float ex = fminf(fmaxf(r.x, bx0), bx0 + 7.f); // nearest box point to the centre
-    const float ey = fminf(fmaxf(r.y, by0), by0 + bh);
+    const float ey = fminf(fmaxf(r.y, by0), by0 + 7.f);
     const bool out_x = ex != r.x, out_y = ey != r.y;
     if (!out_x && !out_y) return true;
     float best = 3.0e38f;
     if (out_x) { // edge x = ex: minimise over y in [by0, by0 + 7]
         const float dx = r.x - ex;
-        const float y = fminf(fmaxf(r.y + r.cxy * dx / r.cyy, by0), by0 + bh);
+        const float y = fminf(fmaxf(r.y + r.cxy * dx / r.cyy, by0), by0 + 7.f);
         const float dy = r.y - y;
         best = r.cxx * dx * dx + 2.f * r.cxy * dx * dy + r.cyy * dy * dy;
     }
@@ -288,15 +286,15 @@ __device__ __forceinline__ void issue_batch(const RasterArgs &a, GeoRec *srec, f
     if (PACK) bulk_g2s(scol4 + buf * BR, a.rcols + bs, (uint32_t)cnt * 16u, &mbar[buf]);
 }
 
-// Culling masks per half-warp: half h of warp w owns the 8 x 4 pixels of rows
-// 4h .. 4h + 3 of w's 8 x 8 block (lanes 16h .. 16h + 15), and its RB*nw-word
-// mask lives at wmask[(2 w + h) RB nw].  limit[2 w + h] (backward) drops
-// records past the half's last contributor.
+// Per-batch culling masks.  Thread tid describes batch slots tid + h NT
+// (h < RB); for every warp w one ballot per slot gives 32 bits of w's
+// RB*nw-word mask (word k covers slots 32k .. 32k+31, so ascending bits are
+// front to back).  limit[w] (backward) drops records past warp w's last
+// contributor.
 template <int RB = 2>
-__device__ __forceinline__ void build_half_masks(const GeoRec *batch, int cnt, int NT, int nw,
-                                                 int wpr, int tile_x0, int tile_y0, int tid,
-                                                 int lane, uint32_t *wmask, int lo = 0,
-                                                 const int32_t *limit = nullptr) {
+__device__ __forceinline__ void build_masks(const GeoRec *batch, int cnt, int lo, int NT, int nw,
+                                            int wpr, int tile_x0, int tile_y0, int tid, int lane,
+                                            uint32_t *wmask, const int32_t *limit) {
 #pragma unroll
     for (int half = 0; half < RB; ++half) {
         const int s = tid + half * NT;
@@ -311,13 +309,10 @@ __device__ __forceinline__ void build_half_masks(const GeoRec *batch, int cnt, i
         for (int w = 0; w < nw; ++w) {
             const float x0 = (float)(tile_x0 + (w % wpr) * 8) + 0.5f;
             const float y0 = (float)(tile_y0 + (w / wpr) * 8) + 0.5f;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                bool ov = valid && ellipse_hits_box(r, pd, x0, y0 + 4.f * h, 3.f);
-                if (limit) ov = ov && (lo + s <= limit[2 * w + h]);
-                const uint32_t bits = __ballot_sync(0xffffffffu, ov);
-                if (lane == 0) wmask[(2 * w + h) * RB * nw + word] = bits;
-            }
+            bool ov = valid && ellipse_hits_box(r, pd, x0, y0);
+            if (limit) ov = ov && (lo + s <= limit[w]);
+            const uint32_t bits = __ballot_sync(0xffffffffu, ov);
+            if (lane == 0) wmask[w * RB * nw + word] = bits;
         }
     }
 }
@@ -352,7 +347,7 @@ __device__ __forceinline__ void blend_pair(const GeoRec &q, const float (&col)[C
                                            float2 npy, float2 &T, float2 (&acc)[CD],
                                            int32_t &cur0, int32_t &cur1, bool &d0, bool &d1,
                                            int32_t idx, uint32_t &n_contrib, int32_t &term0,
-                                           int32_t &term1, bool live = true) {
+                                           int32_t &term1) {
     const float dx = q.x - px;
     const float2 dy = __fadd2_rn(make_float2(q.y, q.y), npy);
     const float A = q.cxx * dx * dx;
@@ -360,8 +355,8 @@ __device__ __forceinline__ void blend_pair(const GeoRec &q, const float (&col)[C
     float2 s = __fmul2_rn(make_float2(q.cyy, q.cyy), dy);
     s = __ffma2_rn(s, dy, make_float2(A, A));
     s = __ffma2_rn(make_float2(B, B), dy, s);
-    const bool v0 = live && !d0 && !(s.x < 0.f || s.x >= 1.f);
-    const bool v1 = live && !d1 && !(s.y < 0.f || s.y >= 1.f);
+    const bool v0 = !d0 && !(s.x < 0.f || s.x >= 1.f);
+    const bool v1 = !d1 && !(s.y < 0.f || s.y >= 1.f);
     if (!__any_sync(0xffffffffu, v0 || v1)) return;
     const float2 om = __ffma2_rn(s, make_float2(-1.f, -1.f), make_float2(1.f, 1.f));
     const float2 l = make_float2(__log2f(om.x), __log2f(om.y));
@@ -489,8 +484,8 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_fwd_kernel(
             const bool ok = mbar_wait_bounded(&mbar[buf], (b >> 1) & 1);
             if (tid == 0 && ok) waited = b + 1;
             const GeoRec *batch = srec + buf * BR;
-            build_half_masks<RB>(batch, cnt, NT, nw, wpr, tx * a.TS, ty * a.TS, tid, lane,
-                                 wmask);
+            build_masks<RB>(batch, cnt, 0, NT, nw, wpr, tx * a.TS, ty * a.TS, tid, lane, wmask,
+                            nullptr);
             if (!PACK) {
 #pragma unroll
                 for (int half = 0; half < RB; ++half) {
@@ -507,33 +502,24 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_fwd_kernel(
                 d0 = d1 = true;
                 break;
             }
-            // Each half-warp walks its own front-to-back list of the records
-            // that can reach its 8 x 4 pixels; one iteration serves the next
-            // record of both halves, so a record reaching one half only takes
-            // half an iteration.  Every pixel still sees, in order, every
-            // record that can cover it.  A half whose pixels are all done
-            // stops consuming its list.
-            {
-                const int hw = lane >> 4, KW = RB * nw;
-                const uint32_t *hm = wmask + (2 * warp + hw) * KW;
-                int k = 0;
-                uint32_t m = hm[0];
-                while (true) {
-                    while (m == 0 && k + 1 < KW) m = hm[++k];
-                    const uint32_t dm = __ballot_sync(0xffffffffu, d0 && d1);
-                    const bool half_done = ((dm >> (16 * hw)) & 0xffffu) == 0xffffu;
-                    const bool has = m != 0 && !half_done;
-                    if (!__any_sync(0xffffffffu, has)) break;
-                    int t = 0;
-                    if (has) {
-                        t = k * 32 + __ffs(m) - 1;
+            if (!__all_sync(0xffffffffu, d0 && d1)) {
+                bool warp_done = false;
+                for (int k = 0; k < RB * nw && !warp_done; ++k) {
+                    uint32_t m = wmask[warp * RB * nw + k];
+                    while (m) {
+                        const int bit = __ffs(m) - 1;
                         m &= m - 1;
+                        const int t = k * 32 + bit;
+                        const GeoRec q = batch[t];
+                        float col[CD];
+                        load_color<CD, PACK>(scol4, scol, buf * BR + t, col);
+                        blend_pair<CD, COUNT>(q, col, px, npy, T, acc, cur0, cur1, d0, d1,
+                                              bs + t, n_contrib, term0, term1);
+                        if (__all_sync(0xffffffffu, d0 && d1)) {
+                            warp_done = true;
+                            break;
+                        }
                     }
-                    const GeoRec q = batch[t];
-                    float col[CD];
-                    load_color<CD, PACK>(scol4, scol, buf * BR + t, col);
-                    blend_pair<CD, COUNT>(q, col, px, npy, T, acc, cur0, cur1, d0, d1, bs + t,
-                                          n_contrib, term0, term1, has);
                 }
             }
             if (__syncthreads_count(d0 && d1) == NT) break;
@@ -629,7 +615,7 @@ __device__ __forceinline__ void bwd_pair_init(BwdPair<CD> &s, const RasterArgs &
 template <int CD>
 __device__ __forceinline__ bool grad_pair(const GeoRec &q, const float (&col)[CD], float px,
                                           float2 npy, int32_t idx, BwdPair<CD> &s,
-                                          float (&g)[7 + CD], bool live = true) {
+                                          float (&g)[7 + CD]) {
     const float dx = q.x - px;
     const float2 dy = __fadd2_rn(make_float2(q.y, q.y), npy);
     const float A = q.cxx * dx * dx;
@@ -637,8 +623,8 @@ __device__ __forceinline__ bool grad_pair(const GeoRec &q, const float (&col)[CD
     float2 sg = __fmul2_rn(make_float2(q.cyy, q.cyy), dy);
     sg = __ffma2_rn(sg, dy, make_float2(A, A));
     sg = __ffma2_rn(make_float2(B, B), dy, sg);
-    const bool v0 = live && s.in0 && idx <= s.bin0 && !(sg.x < 0.f || sg.x >= 1.f);
-    const bool v1 = live && s.in1 && idx <= s.bin1 && !(sg.y < 0.f || sg.y >= 1.f);
+    const bool v0 = s.in0 && idx <= s.bin0 && !(sg.x < 0.f || sg.x >= 1.f);
+    const bool v1 = s.in1 && idx <= s.bin1 && !(sg.y < 0.f || sg.y >= 1.f);
     if (!__any_sync(0xffffffffu, v0 || v1)) return false;
     float2 om = __ffma2_rn(sg, make_float2(-1.f, -1.f), make_float2(1.f, 1.f));
     om.x = v0 ? om.x : 1.f;
@@ -697,24 +683,22 @@ __device__ __forceinline__ float record_scale(int u, float opac, float beta) {
     return 1.f;
 }
 
-// Sums g[OFF .. OFF+REM) over each group of W lanes (the warp, or each
-// half-warp) in power-of-two chunks and adds each group total once into the
-// group's record's shared accumulator.
-template <int OFF, int REM, int W = 32> struct ReduceChunks {
+// Sums g[OFF .. OFF+REM) over the warp in power-of-two chunks and adds each
+// total once into the record's shared accumulator.
+template <int OFF, int REM> struct ReduceChunks {
     template <int NV>
     static __device__ __forceinline__ void run(const float (&g)[NV], int lane, float *acc) {
-        constexpr int R = REM >= 32 ? 32 : REM >= 16 ? 16 : REM >= 8 ? 8 : REM >= 4 ? 4
+        constexpr int S = REM >= 32 ? 32 : REM >= 16 ? 16 : REM >= 8 ? 8 : REM >= 4 ? 4
                                                                          : REM >= 2 ? 2 : 1;
-        constexpr int S = R < W ? R : W;
         float v[S];
 #pragma unroll
         for (int i = 0; i < S; ++i) v[i] = g[OFF + i];
-        const float tot = tr_reduce<S, W>(v, lane);
-        if ((lane & (W / S - 1)) == 0 && tot != 0.f) atomicAdd(&acc[OFF + tr_index<S, W>(lane)], tot);
-        ReduceChunks<OFF + S, REM - S, W>::run(g, lane, acc);
+        const float tot = tr_reduce<S>(v, lane);
+        if ((lane & (32 / S - 1)) == 0 && tot != 0.f) atomicAdd(&acc[OFF + tr_index<S>(lane)], tot);
+        ReduceChunks<OFF + S, REM - S>::run(g, lane, acc);
     }
 };
-template <int OFF, int W> struct ReduceChunks<OFF, 0, W> {
+template <int OFF> struct ReduceChunks<OFF, 0> {
     template <int NV>
     static __device__ __forceinline__ void run(const float (&)[NV], int, float *) {}
 };
@@ -763,11 +747,9 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_bwd_kernel(
     BwdPair<CD> sp;
     bwd_pair_init<CD>(sp, a, pix0, pix1, in0, in1, bg);
 
-    // each half-warp's last contributor (max over its 16 lanes)
-    int32_t wb = max(in0 ? sp.bin0 : INT32_MIN, in1 ? sp.bin1 : INT32_MIN);
-#pragma unroll
-    for (int o = 8; o > 0; o >>= 1) wb = max(wb, __shfl_xor_sync(0xffffffffu, wb, o));
-    if ((lane & 15) == 0) wbin[2 * warp + (lane >> 4)] = wb;
+    const int32_t wb = __reduce_max_sync(
+        0xffffffffu, max(in0 ? sp.bin0 : INT32_MIN, in1 ? sp.bin1 : INT32_MIN));
+    if (lane == 0) wbin[warp] = wb;
     for (int t = tid; t < BR * NV; t += NT) gacc[t] = 0.f;
     for (int t = tid; t < BR; t += NT) touched[t] = 0;
     const bool gather = PACK && a.keys != nullptr;
@@ -780,7 +762,7 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_bwd_kernel(
     }
     __syncthreads();
     int32_t block_bin = INT32_MIN;
-    for (int w = 0; w < 2 * nw; ++w) block_bin = max(block_bin, wbin[w]);
+    for (int w = 0; w < nw; ++w) block_bin = max(block_bin, wbin[w]);
     const int32_t hi_end = max(rs, min(re, block_bin + 1)); // exclusive upper index
     const int nb = (hi_end - rs + BR - 1) / BR;
 
@@ -840,8 +822,8 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_bwd_kernel(
                                ? make_float3(batch[tid + NT].cxx, batch[tid + NT].cxy,
                                              batch[tid + NT].cyy)
                                : make_float3(0.f, 0.f, 0.f);
-        build_half_masks<RB>(batch, cnt, NT, nw, wpr, tx * a.TS, ty * a.TS, tid, lane, wmask,
-                             lo, wbin);
+        build_masks<RB>(batch, cnt, lo, NT, nw, wpr, tx * a.TS, ty * a.TS, tid, lane, wmask,
+                        wbin);
         if (!PACK) {
 #pragma unroll
             for (int half = 0; half < RB; ++half) {
@@ -857,33 +839,20 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_bwd_kernel(
             if (tid == 0) atomicOr(a.status, DEV_ERR_WAIT_TIMEOUT);
             break;
         }
-        // back to front, each half-warp through its own list (as in the
-        // forward): one iteration serves the next record of both halves;
-        // each half reduces over its 16 lanes and adds into its record's
-        // accumulator (both halves add when they hold the same record)
-        {
-            const int hw = lane >> 4, KW = RB * nw;
-            const uint32_t *hm = wmask + (2 * warp + hw) * KW;
-            int k = KW - 1;
-            uint32_t m = hm[k];
-            while (true) {
-                while (m == 0 && k > 0) m = hm[--k];
-                const bool has = m != 0;
-                if (!__any_sync(0xffffffffu, has)) break;
-                int t = 0;
-                if (has) {
-                    const int bit = 31 - __clz(m);
-                    m &= ~(1u << bit);
-                    t = k * 32 + bit;
-                }
+        for (int k = RB * nw - 1; k >= 0; --k) {
+            uint32_t m = wmask[warp * RB * nw + k];
+            while (m) {
+                const int bit = 31 - __clz(m);
+                m &= ~(1u << bit);
+                const int t = k * 32 + bit;
                 const int32_t idx = lo + t;
                 const GeoRec q = batch[t];
                 float col[CD];
                 load_color<CD, PACK>(scol4, scol, buf * BR + t, col);
                 float g[NV];
-                if (!grad_pair<CD>(q, col, px, npy, idx, sp, g, has)) continue;
-                ReduceChunks<0, NV, 16>::run(g, lane, gacc + t * NV);
-                if ((lane & 15) == 0 && has) touched[t] = 1;
+                if (!grad_pair<CD>(q, col, px, npy, idx, sp, g)) continue;
+                ReduceChunks<0, NV>::run(g, lane, gacc + t * NV);
+                if (lane == 0) touched[t] = 1;
             }
         }
         __syncthreads();

@@ -145,44 +145,41 @@ __device__ __forceinline__ float warp_transpose_reduce16(float (&v)[16], int lan
     return v[0];
 }
 
-// Generalised transpose reduction of S = 2^m values (1 <= S <= W) over groups
-// of W = 32 or 16 lanes (a whole warp, or each half-warp on its own): m
-// halving steps (each lane keeps half of its slots and adds its partner's
-// other half) then log2(W) - m plain butterfly steps, all inside the group.
-// Lane L returns its group's total of value tr_index<S, W>(L); lanes with
-// L % (W / S) == 0 hold each value exactly once.
-template <int S, int W = 32> __device__ __forceinline__ int tr_index(int lane) {
-    int idx = 0, n = S, h = W / 2;
+// Generalised transpose reduction of S = 2^m values (1 <= S <= 32) over the 32
+// lanes: m halving steps (each lane keeps half of its slots and adds its
+// partner's other half) then 5 - m plain butterfly steps.  Lane L returns the
+// warp total of value tr_index<S>(L); lanes with L % (32 / S) == 0 hold each
+// value exactly once.
+template <int S> __device__ __forceinline__ int tr_index(int lane) {
+    int idx = 0, n = S, h = 16;
 #pragma unroll
     for (int step = 0; step < 5; ++step) {
-        if (h >= 1 && n > 1) {
+        if (n > 1) {
             if (lane & h) idx += n / 2;
             n >>= 1;
+            h >>= 1;
         }
-        h >>= 1;
     }
     return idx;
 }
-template <int S, int W = 32> __device__ __forceinline__ float tr_reduce(float (&v)[S], int lane) {
+template <int S> __device__ __forceinline__ float tr_reduce(float (&v)[S], int lane) {
     const unsigned full = 0xffffffffu;
-    int n = S, h = W / 2;
+    int n = S, h = 16;
 #pragma unroll
     for (int step = 0; step < 5; ++step) {
-        if (h >= 1) {
-            if (n > 1) {
-                const bool hi = lane & h;
+        if (n > 1) {
+            const bool hi = lane & h;
 #pragma unroll
-                for (int i = 0; i < S / 2; ++i) {
-                    if (i < n / 2) {
-                        const float send = hi ? v[i] : v[i + n / 2];
-                        const float keep = hi ? v[i + n / 2] : v[i];
-                        v[i] = keep + __shfl_xor_sync(full, send, h);
-                    }
+            for (int i = 0; i < S / 2; ++i) {
+                if (i < n / 2) {
+                    const float send = hi ? v[i] : v[i + n / 2];
+                    const float keep = hi ? v[i + n / 2] : v[i];
+                    v[i] = keep + __shfl_xor_sync(full, send, h);
                 }
-                n >>= 1;
-            } else {
-                v[0] += __shfl_xor_sync(full, v[0], h);
             }
+            n >>= 1;
+        } else {
+            v[0] += __shfl_xor_sync(full, v[0], h);
         }
         h >>= 1;
     }
