@@ -21,8 +21,11 @@
 //     bitmasks by ballot, so a warp only visits records that can touch its
 //     pixels;
 //   * the backward sums the 7 + channels gradients of a record over a warp with
-//     transpose reductions (14 shuffles for 10 values), accumulates warps in
-//     shared memory and issues one global atomic per (tile, record, value).
+//     transpose reductions (14 shuffles for 10 values), each warp writes its
+//     totals into its own list of rows in shared memory with plain stores, and
+//     per batch the rows of a record are summed and added to its gradient row
+//     with three 16-byte vector atomics (fused path) or one scalar atomic per
+//     value (drop-in arrays).
 #include <atomic>
 #include <cstdio>
 
@@ -38,6 +41,7 @@ struct __align__(16) GeoRec {
 static_assert(sizeof(GeoRec) == 32, "GeoRec must be 32 bytes");
 
 constexpr uint32_t DEV_ERR_BAD_INDEX = 8u;
+constexpr int GRAD_ROW = 12; // floats per gradient row (7 + up to 5 channels)
 
 struct RasterArgs {
     int C, W, H, TS, TW, TH, n_tiles;
@@ -58,6 +62,10 @@ struct RasterArgs {
     const float *v_out_c;
     const float *v_out_a;
     float *v_m2, *v_cn, *v_col, *v_op, *v_be;
+    // or, when not null, one gradient row per entry instead of the five arrays:
+    // [v_xy(2), v_conic(3), v_opacity, v_beta, v_colour(CD), 0...], GRAD_ROW
+    // floats (16-byte aligned rows, added with vector atomics)
+    float *v_rows;
     uint32_t *status;
     // counters of the COUNT forward, or nullptr: [0] contributing (pixel,
     // record) pairs, [1] pairs a per-pixel loop evaluates up to termination,
@@ -164,12 +172,20 @@ __global__ void pack_records_kernel(int64_t T, int64_t n_prims, const int32_t *_
 // the culling phase (RB = 1 in the backward of tiles up to 16 x 16 with packed
 // colours of at most 4 channels, whose smaller shared footprint lets 8 CTAs
 // share an SM; else 2).
+// The backward accumulates a batch's per-record gradient sums in one of two
+// ways.  KE = 0: one shared accumulator row per batch slot (BR x NV floats),
+// which every warp adds its reduced sums to with shared-memory atomics, and a
+// touched flag per slot.  KE > 0: every warp owns a list of KE entry rows
+// (NV floats each) that it fills with plain stores, one row per record it
+// visits, and a byte per batch slot naming the row (0xFF: none); the flush
+// sums the warps' rows of a slot.  Shared float atomics cost about as much as
+// the rest of a visit's reduction, so the small tiles use the lists.
 struct SmemLayout {
     int mask_off, rec_off, col_off, gacc_off, touched_off, total;
 };
 
 template <int CD, bool PACK, bool BWD>
-__host__ __device__ inline SmemLayout smem_layout(int NT, int RB = 2) {
+__host__ __device__ inline SmemLayout smem_layout(int NT, int RB = 2, int KE = 0) {
     constexpr int NV = 7 + CD; // gradient values per record
     const int nw = NT / 32, BR = RB * NT;
     SmemLayout L;
@@ -179,8 +195,13 @@ __host__ __device__ inline SmemLayout smem_layout(int NT, int RB = 2) {
     const int colbytes = PACK ? 16 : CD * 4;
     L.col_off = L.rec_off + 2 * BR * (int)sizeof(GeoRec);
     L.gacc_off = (L.col_off + 2 * BR * colbytes + 15) & ~15;
-    L.touched_off = L.gacc_off + (BWD ? BR * NV * 4 : 0);
-    L.total = L.touched_off + (BWD ? BR * 4 : 0);
+    if (BWD && KE > 0) {
+        L.touched_off = L.gacc_off + nw * KE * NV * 4; // entry rows, then the slot maps
+        L.total = L.touched_off + nw * BR;
+    } else {
+        L.touched_off = L.gacc_off + (BWD ? BR * NV * 4 : 0);
+        L.total = L.touched_off + (BWD ? BR * 4 : 0);
+    }
     return L;
 }
 
@@ -340,8 +361,10 @@ __device__ __forceinline__ void load_color(const float4 *scol4, const float *sco
 // __fadd2_rn, __fmul2_rn: per component the same rounding as the scalar
 // operations); (1 - sigma)^beta is formed as 2^(beta log2(1 - sigma)).  The
 // updates are select-based so that a warp issues them once for both pixels
-// and all lanes; lanes whose record is skipped evaluate dummies that the
-// selects discard.
+// and all lanes; lanes whose record is skipped evaluate dummies (NaN where
+// sigma >= 1) that the selects discard.  Records no lane can use are
+// evaluated the same way rather than skipped after a warp vote: under 1% of
+// the culled visits are such.
 template <int CD, bool COUNT>
 __device__ __forceinline__ void blend_pair(const GeoRec &q, const float (&col)[CD], float px,
                                            float2 npy, float2 &T, float2 (&acc)[CD],
@@ -357,7 +380,6 @@ __device__ __forceinline__ void blend_pair(const GeoRec &q, const float (&col)[C
     s = __ffma2_rn(make_float2(B, B), dy, s);
     const bool v0 = !d0 && !(s.x < 0.f || s.x >= 1.f);
     const bool v1 = !d1 && !(s.y < 0.f || s.y >= 1.f);
-    if (!__any_sync(0xffffffffu, v0 || v1)) return;
     const float2 om = __ffma2_rn(s, make_float2(-1.f, -1.f), make_float2(1.f, 1.f));
     const float2 l = make_float2(__log2f(om.x), __log2f(om.y));
     const float2 e = __fmul2_rn(l, make_float2(q.beta, q.beta));
@@ -606,14 +628,15 @@ __device__ __forceinline__ void bwd_pair_init(BwdPair<CD> &s, const RasterArgs &
 // sigma chain when opacity (1 - sigma)^beta <= 0.999), packed two-wide (one
 // FP32x2 instruction per step for the pixel pair); valid lanes are inside,
 // at or before their last contributor, with sigma in [0, 1), others evaluate
-// finite dummies (1 - sigma replaced by 1) that selects zero.  Returns
-// whether any lane of the warp had a valid pixel.  g receives the pair's sums
+// finite dummies (1 - sigma replaced by 1) that selects zero.  A record no
+// lane can use is evaluated too: under 1% of the culled visits are such, and
+// a warp vote to skip them cost more than it saved.  g receives the pair's sums
 //   [w dx, w dy, w dx^2, w dx dy, w dy^2, vis v_alpha, vis v_alpha log2(1-s),
 //    fac v_colour (CD)],  w = v_alpha (1 - sigma)^(beta - 1),
 // turned into [v_xy, v_conic, v_opacity, v_beta, v_colour] per record at
 // the flush (the conic, -opacity beta and opacity ln 2 factors).
 template <int CD>
-__device__ __forceinline__ bool grad_pair(const GeoRec &q, const float (&col)[CD], float px,
+__device__ __forceinline__ void grad_pair(const GeoRec &q, const float (&col)[CD], float px,
                                           float2 npy, int32_t idx, BwdPair<CD> &s,
                                           float (&g)[7 + CD]) {
     const float dx = q.x - px;
@@ -625,7 +648,6 @@ __device__ __forceinline__ bool grad_pair(const GeoRec &q, const float (&col)[CD
     sg = __ffma2_rn(make_float2(B, B), dy, sg);
     const bool v0 = s.in0 && idx <= s.bin0 && !(sg.x < 0.f || sg.x >= 1.f);
     const bool v1 = s.in1 && idx <= s.bin1 && !(sg.y < 0.f || sg.y >= 1.f);
-    if (!__any_sync(0xffffffffu, v0 || v1)) return false;
     float2 om = __ffma2_rn(sg, make_float2(-1.f, -1.f), make_float2(1.f, 1.f));
     om.x = v0 ? om.x : 1.f;
     om.y = v1 ? om.y : 1.f;
@@ -669,55 +691,75 @@ __device__ __forceinline__ bool grad_pair(const GeoRec &q, const float (&col)[CD
     s.S = __ffma2_rn(fac, cv, s.S);
     s.T.x = v0 ? Tn.x : s.T.x;
     s.T.y = v1 ? Tn.y : s.T.y;
-    return true;
 }
 
 // Factor turning the reduced sum g[u] (u >= 2) of a record into its gradient
 // value u of [v_xy(2), v_conic(3), v_opacity, v_beta, v_colour(CD)]; v_xy is
-// -2 opacity beta (conic [w dx, w dy]) and is formed at the flush.
-__device__ __forceinline__ float record_scale(int u, float opac, float beta) {
+// -2 opacity beta (conic [w dx, w dy]) and is formed at the flush.  With
+// the entry lists the first two sums are multiplied by the conic per lane
+// before the reduction, so every value is a factor times its sum
+// (pre_conic = true).
+__device__ __forceinline__ float record_scale(int u, float opac, float beta,
+                                              bool pre_conic = false) {
     const float ob = opac * beta;
-    if (u == 3) return -2.f * ob;
+    if (u == 3 || (pre_conic && u < 2)) return -2.f * ob;
     if (u < 5) return -ob;
     if (u == 6) return opac * 0.6931471805599453f;
     return 1.f;
 }
 
-// Sums g[OFF .. OFF+REM) over the warp in power-of-two chunks and adds each
-// total once into the record's shared accumulator.
+// Gradient array element of value u of primitive entry gid.
+template <int CD>
+__device__ __forceinline__ float *grad_dst(const RasterArgs &a, int u, int64_t gid) {
+    if (a.v_rows) return a.v_rows + gid * GRAD_ROW + u;
+    if (u < 2) return a.v_m2 + 2 * gid + u;
+    if (u < 5) return a.v_cn + 3 * gid + (u - 2);
+    if (u == 5) return a.v_op + gid;
+    if (u == 6) return a.v_be + gid;
+    return a.v_col + gid * CD + (u - 7);
+}
+
+// Sums g[OFF .. OFF+REM) over the warp in power-of-two chunks; every lane
+// calls sink(u, total, owner) for the value u whose total it holds, owner
+// being true for exactly one lane per value.
 template <int OFF, int REM> struct ReduceChunks {
-    template <int NV>
-    static __device__ __forceinline__ void run(const float (&g)[NV], int lane, float *acc) {
+    template <int NV, class Sink>
+    static __device__ __forceinline__ void run(const float (&g)[NV], const LaneMasks &lm, int lane,
+                                               Sink &sink) {
         constexpr int S = REM >= 32 ? 32 : REM >= 16 ? 16 : REM >= 8 ? 8 : REM >= 4 ? 4
                                                                          : REM >= 2 ? 2 : 1;
         float v[S];
 #pragma unroll
         for (int i = 0; i < S; ++i) v[i] = g[OFF + i];
-        const float tot = tr_reduce<S>(v, lane);
-        if ((lane & (32 / S - 1)) == 0 && tot != 0.f) atomicAdd(&acc[OFF + tr_index<S>(lane)], tot);
-        ReduceChunks<OFF + S, REM - S>::run(g, lane, acc);
+        const float tot = tr_reduce<S>(v, lm);
+        sink(OFF + tr_index<S>(lane), tot, (lane & (32 / S - 1)) == 0);
+        ReduceChunks<OFF + S, REM - S>::run(g, lm, lane, sink);
     }
 };
 template <int OFF> struct ReduceChunks<OFF, 0> {
-    template <int NV>
-    static __device__ __forceinline__ void run(const float (&)[NV], int, float *) {}
+    template <int NV, class Sink>
+    static __device__ __forceinline__ void run(const float (&)[NV], const LaneMasks &, int,
+                                               Sink &) {}
 };
 
-// MINB > 1: tiles of at most 128 threads, MINB CTAs per SM.
-template <int CD, bool PACK, int RB, int MINB>
+// MINB > 1: tiles of at most 128 threads, MINB CTAs per SM.  KE > 0: entry
+// lists of KE rows per warp (see smem_layout).
+template <int CD, bool PACK, int RB, int MINB, int KE>
 __global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_bwd_kernel(RasterArgs a) {
     constexpr int NV = 7 + CD;
+    static_assert(KE < 255, "entry rows are named by a byte");
     extern __shared__ __align__(128) unsigned char sm[];
     const int NT = blockDim.x, nw = NT >> 5, BR = RB * NT;
-    const SmemLayout L = smem_layout<CD, PACK, true>(NT, RB);
+    const SmemLayout L = smem_layout<CD, PACK, true>(NT, RB, KE);
     uint64_t *mbar = reinterpret_cast<uint64_t *>(sm);
     uint32_t *wmask = reinterpret_cast<uint32_t *>(sm + L.mask_off);
     int32_t *wbin = reinterpret_cast<int32_t *>(sm + L.mask_off + nw * RB * nw * 4);
     GeoRec *srec = reinterpret_cast<GeoRec *>(sm + L.rec_off);
     float4 *scol4 = reinterpret_cast<float4 *>(sm + L.col_off);
     float *scol = reinterpret_cast<float *>(sm + L.col_off);
-    float *gacc = reinterpret_cast<float *>(sm + L.gacc_off);
+    float *gacc = reinterpret_cast<float *>(sm + L.gacc_off);       // KE > 0: entry rows
     int32_t *touched = reinterpret_cast<int32_t *>(sm + L.touched_off);
+    uint8_t *slot_row = reinterpret_cast<uint8_t *>(sm + L.touched_off); // KE > 0
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int bt = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;
@@ -750,8 +792,12 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_bwd_kernel(
     const int32_t wb = __reduce_max_sync(
         0xffffffffu, max(in0 ? sp.bin0 : INT32_MIN, in1 ? sp.bin1 : INT32_MIN));
     if (lane == 0) wbin[warp] = wb;
-    for (int t = tid; t < BR * NV; t += NT) gacc[t] = 0.f;
-    for (int t = tid; t < BR; t += NT) touched[t] = 0;
+    if (KE > 0) {
+        for (int t = tid; t < nw * BR; t += NT) slot_row[t] = 0xFF;
+    } else {
+        for (int t = tid; t < BR * NV; t += NT) gacc[t] = 0.f;
+        for (int t = tid; t < BR; t += NT) touched[t] = 0;
+    }
     const bool gather = PACK && a.keys != nullptr;
     const int64_t lo_e = gather ? (int64_t)cam * a.n_per_view : 0;
     const int64_t hi_e = lo_e + a.n_per_view - 1;
@@ -766,6 +812,7 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_bwd_kernel(
     const int32_t hi_end = max(rs, min(re, block_bin + 1)); // exclusive upper index
     const int nb = (hi_end - rs + BR - 1) / BR;
 
+    const LaneMasks lm = lane_masks(lane);
     // batch b covers [max(rs, hi_end - (b + 1) BR), hi_end - b BR): back to front
     int issued = 0, waited = 0;
     int32_t ent[RB];
@@ -839,6 +886,7 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_bwd_kernel(
             if (tid == 0) atomicOr(a.status, DEV_ERR_WAIT_TIMEOUT);
             break;
         }
+        int rows = 0; // KE > 0: entry rows this warp has filled in this batch
         for (int k = RB * nw - 1; k >= 0; --k) {
             uint32_t m = wmask[warp * RB * nw + k];
             while (m) {
@@ -850,12 +898,80 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_bwd_kernel(
                 float col[CD];
                 load_color<CD, PACK>(scol4, scol, buf * BR + t, col);
                 float g[NV];
-                if (!grad_pair<CD>(q, col, px, npy, idx, sp, g)) continue;
-                ReduceChunks<0, NV>::run(g, lane, gacc + t * NV);
-                if (lane == 0) touched[t] = 1;
+                grad_pair<CD>(q, col, px, npy, idx, sp, g);
+                if constexpr (KE > 0) {
+                    const float g0 = g[0], g1 = g[1];
+                    g[0] = q.cxx * g0 + q.cxy * g1;
+                    g[1] = q.cxy * g0 + q.cyy * g1;
+                    if (rows < KE) {
+                        float *row = gacc + (warp * KE + rows) * NV;
+                        // every lane of a group holds the same total: all store it
+                        auto put = [row](int u, float tot, bool) { row[u] = tot; };
+                        ReduceChunks<0, NV>::run(g, lm, lane, put);
+                        if (lane == 0) slot_row[warp * BR + t] = (uint8_t)rows;
+                        ++rows;
+                    } else { // list full: this record's sums go straight to the arrays
+                        auto add = [&](int u, float tot, bool owner) {
+                            if (owner && tot != 0.f)
+                                atomicAdd(grad_dst<CD>(a, u, q.gid),
+                                          record_scale(u, q.opac, q.beta, true) * tot);
+                        };
+                        ReduceChunks<0, NV>::run(g, lm, lane, add);
+                    }
+                } else {
+                    float *acc = gacc + t * NV;
+                    auto add = [acc](int u, float tot, bool owner) {
+                        if (owner && tot != 0.f) atomicAdd(&acc[u], tot);
+                    };
+                    ReduceChunks<0, NV>::run(g, lm, lane, add);
+                    if (lane == 0) touched[t] = 1;
+                }
             }
         }
         __syncthreads();
+        if constexpr (KE > 0) {
+#pragma unroll
+            for (int half = 0; half < RB; ++half) {
+                const int sl = tid + half * NT;
+                if (sl >= cnt) continue;
+                float sum[NV];
+                bool any = false;
+#pragma unroll
+                for (int u = 0; u < NV; ++u) sum[u] = 0.f;
+                for (int w = 0; w < nw; ++w) {
+                    const int r = slot_row[w * BR + sl];
+                    if (r == 0xFF) continue;
+                    slot_row[w * BR + sl] = 0xFF;
+                    any = true;
+                    const float *row = gacc + (w * KE + r) * NV;
+#pragma unroll
+                    for (int u = 0; u < NV; ++u) sum[u] += row[u];
+                }
+                if (!any) continue;
+                const int64_t gg = half ? gid1 : gid0;
+                const float op = half ? op1 : op0, be = half ? be1 : be0;
+#pragma unroll
+                for (int u = 0; u < NV; ++u) sum[u] *= record_scale(u, op, be, true);
+                if (NV <= GRAD_ROW && a.v_rows) {
+                    // three 16-byte vector atomics per row instead of NV scalar ones
+                    float4 *row = reinterpret_cast<float4 *>(a.v_rows + gg * GRAD_ROW);
+#pragma unroll
+                    for (int c = 0; c < (NV + 3) / 4; ++c) {
+                        float4 v;
+                        v.x = sum[4 * c];
+                        v.y = 4 * c + 1 < NV ? sum[(4 * c + 1) % NV] : 0.f;
+                        v.z = 4 * c + 2 < NV ? sum[(4 * c + 2) % NV] : 0.f;
+                        v.w = 4 * c + 3 < NV ? sum[(4 * c + 3) % NV] : 0.f;
+                        atomicAdd(row + c, v);
+                    }
+                } else {
+#pragma unroll
+                    for (int u = 0; u < NV; ++u)
+                        if (sum[u] != 0.f) atomicAdd(grad_dst<CD>(a, u, gg), sum[u]);
+                }
+            }
+            continue;
+        }
 #pragma unroll
         for (int half = 0; half < RB; ++half) {
             const int sl = tid + half * NT;
@@ -870,15 +986,7 @@ __global__ void __launch_bounds__(MINB > 1 ? 128 : 512, MINB) raster_bwd_kernel(
 #pragma unroll
                 for (int u = 0; u < NV; ++u) {
                     const float val = u == 0 ? m0 : u == 1 ? m1 : ga[u] * record_scale(u, op, be);
-                    if (val != 0.f) {
-                        float *dst;
-                        if (u < 2) dst = a.v_m2 + 2 * gg + u;
-                        else if (u < 5) dst = a.v_cn + 3 * gg + (u - 2);
-                        else if (u == 5) dst = a.v_op + gg;
-                        else if (u == 6) dst = a.v_be + gg;
-                        else dst = a.v_col + gg * CD + (u - 7);
-                        atomicAdd(dst, val);
-                    }
+                    if (val != 0.f) atomicAdd(grad_dst<CD>(a, u, gg), val);
                     ga[u] = 0.f;
                 }
                 touched[sl] = 0;
@@ -925,16 +1033,23 @@ static int launch_pack(int64_t T, int64_t n_prims, const int32_t *fl, const floa
     return check_launch("pack_records");
 }
 
-// Occupancy variants of the 3-channel blend kernels for tiles of at most 128
-// threads (16 x 16 pixels and smaller), selected process-wide by
-// ubs_set_blend_variant: each trades records per staged batch (RB) against
-// CTAs per SM (MINB, the register bound it implies) --
+// Variants of the 3-channel blend kernels for tiles of at most 128 threads
+// (16 x 16 pixels and smaller), selected process-wide by
+// ubs_set_blend_variant.  The forward's trade records per staged batch (RB)
+// against CTAs per SM (MINB, the register bound it implies); the backward's
+// the register bound and the accumulation scheme (see smem_layout) --
 //   forward:  0: RB 2, 8 CTAs/SM;  1: RB 1, 10 CTAs/SM;  2: RB 2, 6 CTAs/SM
-//   backward: 0: RB 1, 8 CTAs/SM;  1: RB 2, 6 CTAs/SM;   2: RB 1, 6 CTAs/SM
+//   backward: 0: RB 1, 8 CTAs/SM, per-warp row lists of 64 entries;
+//             1: the same at 7 CTAs/SM (72 registers);
+//             2: RB 1, 8 CTAs/SM, shared accumulators with shared atomics
 // Every variant computes the same images; the backward's gradient sums are
-// the same up to the order of their atomic additions.
+// the same up to the order of their additions.
+// A warp that visits more than KE_SMALL records of one 128-record batch adds
+// the rest straight to the gradient arrays; on the 1M-primitive 1080p frame
+// 64 of 5.6M visits do.
 std::atomic<int> g_blend_fwd_variant{0}, g_blend_bwd_variant{0};
 constexpr int kBlendVariants = 3;
+constexpr int KE_SMALL = 64; // backward entry rows per warp in tiles of at most 128 threads
 
 template <int CD, bool BWD>
 static int launch_blend(RasterArgs &a, cudaStream_t st) {
@@ -948,8 +1063,9 @@ static int launch_blend(RasterArgs &a, cudaStream_t st) {
                             ? (BWD ? g_blend_bwd_variant.load() : g_blend_fwd_variant.load())
                             : 0;
     int RB = (small && BWD) ? 1 : 2;
-    if (variant == 1) RB = BWD ? 2 : 1;
-    const SmemLayout L = smem_layout<CD, PACK, BWD>(NT, RB);
+    if (!BWD && variant == 1) RB = 1;
+    const int KE = (BWD && small && !(CD == 3 && variant == 2)) ? KE_SMALL : 0;
+    const SmemLayout L = smem_layout<CD, PACK, BWD>(NT, RB, KE);
     if (L.total > 227 * 1024)
         return set_error(UBS_ERR_UNSUPPORTED, "raster: tile_size %d with %d channels needs %d B "
                                               "of shared memory", a.TS, CD, L.total);
@@ -958,18 +1074,19 @@ static int launch_blend(RasterArgs &a, cudaStream_t st) {
     void (*k)(RasterArgs) = nullptr;
     if constexpr (CD == 3) {
         if (small && variant == 1)
-            k = BWD ? raster_bwd_kernel<3, true, 2, 6> : raster_fwd_kernel<3, true, false, 1, 10>;
+            k = BWD ? raster_bwd_kernel<3, true, 1, 7, KE_SMALL>
+                    : raster_fwd_kernel<3, true, false, 1, 10>;
         else if (small && variant == 2)
-            k = BWD ? raster_bwd_kernel<3, true, 1, 6> : raster_fwd_kernel<3, true, false, 2, 6>;
+            k = BWD ? raster_bwd_kernel<3, true, 1, 8, 0> : raster_fwd_kernel<3, true, false, 2, 6>;
     }
     if constexpr (PACK) {
         if (small && !k)
-            k = BWD ? raster_bwd_kernel<CD, PACK, 1, (CD < 4 ? 8 : 7)>
+            k = BWD ? raster_bwd_kernel<CD, PACK, 1, (CD < 4 ? 8 : 7), KE_SMALL>
                     : (a.pair_count ? raster_fwd_kernel<CD, PACK, true, 2, 8>
                                     : raster_fwd_kernel<CD, PACK, false, 2, 8>);
     }
     if (!k)
-        k = BWD ? raster_bwd_kernel<CD, PACK, 2, 1>
+        k = BWD ? raster_bwd_kernel<CD, PACK, 2, 1, 0>
                 : (a.pair_count ? raster_fwd_kernel<CD, PACK, true, 2, 1>
                                 : raster_fwd_kernel<CD, PACK, false, 2, 1>);
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, L.total) !=
@@ -1069,8 +1186,8 @@ int scene_blend(int fwd, int32_t C, int64_t CN, int32_t n_buckets, int32_t tile_
                 const float *bg, const int32_t *tile_base,
                 const int32_t *dims, const int64_t *pix_base, float *out_c, float *out_a,
                 int32_t *last_ids, const float *render_alphas, const int32_t *last_in,
-                const float *v_out_c, const float *v_out_a, float *v_m2, float *v_cn,
-                float *v_col, float *v_op, float *v_be, uint32_t *status, cudaStream_t st) {
+                const float *v_out_c, const float *v_out_a, float *v_rows, uint32_t *status,
+                cudaStream_t st) {
     RasterArgs a{};
     a.C = C;
     a.TS = tile_size;
@@ -1099,11 +1216,7 @@ int scene_blend(int fwd, int32_t C, int64_t CN, int32_t n_buckets, int32_t tile_
     a.last_in = last_in;
     a.v_out_c = v_out_c;
     a.v_out_a = v_out_a;
-    a.v_m2 = v_m2;
-    a.v_cn = v_cn;
-    a.v_col = v_col;
-    a.v_op = v_op;
-    a.v_be = v_be;
+    a.v_rows = v_rows;
     return launch_blend<3, true>(a, st);
 }
 

@@ -38,8 +38,8 @@ int scene_blend(int fwd, int32_t C, int64_t CN, int32_t n_buckets, int32_t tile_
                 const float *bg, const int32_t *tile_base,
                 const int32_t *dims, const int64_t *pix_base, float *out_c, float *out_a,
                 int32_t *last_ids, const float *render_alphas, const int32_t *last_in,
-                const float *v_out_c, const float *v_out_a, float *v_m2, float *v_cn,
-                float *v_col, float *v_op, float *v_be, uint32_t *status, cudaStream_t st);
+                const float *v_out_c, const float *v_out_a, float *v_rows, uint32_t *status,
+                cudaStream_t st);
 
 // scene_act.cu (compiled with IEEE math): activated scales, betas and
 // opacities, act = [N, D] | [N, D - 2] | [N]
@@ -51,6 +51,8 @@ namespace {
 constexpr int kTileMaxViews = 1 << 16;
 // floats per primitive of the activation section (D + D - 2 + 1, D <= 7)
 constexpr int kActPerPrim = 13;
+// floats per gradient row of the backward blend (GRAD_ROW in raster.cu)
+constexpr int kGradRow = 12;
 
 struct __align__(16) Rec {
     float x, y, opac, beta;
@@ -85,7 +87,9 @@ struct SceneArgs {
     int32_t *bucket_counts;
     uint32_t *status;
     // backward
-    const float *v_m2, *v_cn, *v_col, *v_op, *v_be;
+    // gradient row per (view, primitive) entry from the backward blend:
+    // [v_xy(2), v_conic(3), v_opacity, v_beta, v_rgb(3), 0, 0]
+    const float *v_rows;
     float *g_xyz, *g_mean, *g_scale, *g_ltri, *g_opac, *g_beta, *g_rgb;
     int exact;
 };
@@ -265,6 +269,8 @@ __global__ void __launch_bounds__(PRIM_THREADS, D == 6 ? 8 : 6) scene_prim_fwd_k
     PrimRows rows;
     if (prim_rows<D>(a, idx, n, lane, stage[threadIdx.x >> 5], rows)) __syncwarp();
     if (idx >= (int64_t)a.C * a.N) return;
+    const float4 *vrow = reinterpret_cast<const float4 *>(a.v_rows + idx * kGradRow);
+    const float4 vr0 = vrow[0], vr1 = vrow[1], vr2 = vrow[2];
     PrimFwd<D> f;
     prim_forward<D>(a, rows, v, f);
     const Cam cam = view_cam(a, v);
@@ -397,6 +403,8 @@ template <int D> __global__ void __launch_bounds__(PRIM_THREADS) scene_prim_bwd_
         }
         return;
     }
+    const float4 *vrow = reinterpret_cast<const float4 *>(a.v_rows + idx * kGradRow);
+    const float4 vr0 = vrow[0], vr1 = vrow[1], vr2 = vrow[2];
     PrimFwd<D> f;
     prim_forward<D>(a, rows, v, f);
     const Cam cam = view_cam(a, v);
@@ -404,7 +412,7 @@ template <int D> __global__ void __launch_bounds__(PRIM_THREADS) scene_prim_bwd_
     // projection VJP (fully_fused_projection_bwd.cu:69-174) with the saved conic
     const float4 c1 = reinterpret_cast<const float4 *>(a.recs + idx)[1];
     const float cn[3] = {c1.x, c1.y, c1.z};
-    const float vcn[3] = {a.v_cn[idx * 3], a.v_cn[idx * 3 + 1], a.v_cn[idx * 3 + 2]};
+    const float vcn[3] = {vr0.z, vr0.w, vr1.x};
     float vc2[4];
     conic_vjp(cn, vcn, a.eps2d, false, 0.f, 0.f, vc2);
     float pc[3];
@@ -415,7 +423,7 @@ template <int D> __global__ void __launch_bounds__(PRIM_THREADS) scene_prim_bwd_
 #pragma unroll
     for (int k = 0; k < 9; ++k) vSc.m[k] = 0.f;
     float vpc[3] = {0.f, 0.f, 0.f};
-    persp_vjp(pc, Sc, cam, W, H, vc2, a.v_m2[idx * 2], a.v_m2[idx * 2 + 1], vSc, vpc);
+    persp_vjp(pc, Sc, cam, W, H, vc2, vr0.x, vr0.y, vSc, vpc);
     float gM[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k)
@@ -434,7 +442,7 @@ template <int D> __global__ void __launch_bounds__(PRIM_THREADS) scene_prim_bwd_
     gVc[8] = vSw(2, 2);
     // conditioning VJP (cond_mean_convariance_opacity_bwd.cu:102-563)
     float gm[D], gV[D * D], go, gb[K];
-    cond_backward<K>(f.m, f.V, f.o, f.b, f.q, gM, gVc, a.v_op[idx], a.exact != 0, gm, gV, &go,
+    cond_backward<K>(f.m, f.V, f.o, f.b, f.q, gM, gVc, vr1.y, a.exact != 0, gm, gV, &go,
                      gb);
     // Sigma = L L^T: dL = (gV + gV^T) L (rot_scale_l_triangle_to_covar_bwd.cu)
     float dL[D * D];
@@ -485,11 +493,12 @@ template <int D> __global__ void __launch_bounds__(PRIM_THREADS) scene_prim_bwd_
 #pragma unroll
     for (int k = 0; k < NL; ++k) put(&a.g_ltri[n * NL + k], gl[k]);
     put(&a.g_opac[n], go * f.o * (1.f - f.o));
-    put(&a.g_beta[n * (D - 2)], a.v_be[idx] * f.b0);
+    put(&a.g_beta[n * (D - 2)], vr1.z * f.b0);
 #pragma unroll
     for (int k = 0; k < K; ++k) put(&a.g_beta[n * (D - 2) + 1 + k], gb[k] * f.b[k]);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) put(&a.g_rgb[n * 3 + k], a.v_col[idx * 3 + k]);
+    put(&a.g_rgb[n * 3], vr1.w);
+    put(&a.g_rgb[n * 3 + 1], vr2.x);
+    put(&a.g_rgb[n * 3 + 2], vr2.y);
 }
 
 size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -503,7 +512,7 @@ struct SceneWs {
     int64_t *block_sums;
     uint64_t *keys, *scratch;
     float4 *cols_n;
-    float *grads; // v_m2 (2), v_cn (3), v_col (3), v_op, v_be per (view, primitive)
+    float *grads; // one kGradRow-float gradient row per (view, primitive) entry
     float *act;   // activated parameters (scene_act.cu)
     size_t bytes;
 };
@@ -531,7 +540,7 @@ SceneWs scene_ws(void *base, int32_t C, int64_t N, int32_t nb, int64_t cap) {
     w.keys = reinterpret_cast<uint64_t *>(take(cap * 8));
     w.scratch = reinterpret_cast<uint64_t *>(take(cap * 8));
     w.cols_n = reinterpret_cast<float4 *>(take((size_t)N * 16));
-    w.grads = reinterpret_cast<float *>(take(CN * 10 * 4));
+    w.grads = reinterpret_cast<float *>(take(CN * kGradRow * 4));
     w.act = reinterpret_cast<float *>(take((size_t)N * kActPerPrim * 4));
     w.bytes = o;
     return w;
@@ -723,7 +732,7 @@ int ubs_scene_forward_masked(int32_t dim, int64_t N, const float *xyz, const flo
     return scene_blend(1, C, CN, n_buckets, tile_size, w.offsets, w.order, &w.hdr->total, capacity,
                        w.keys, w.recs, w.cols_n, backgrounds, tile_base, view_dims, pix_base,
                        render_colors, render_alphas, last_ids, nullptr, nullptr, nullptr, nullptr,
-                       nullptr, nullptr, nullptr, nullptr, nullptr, &w.hdr->status, st);
+                       nullptr, &w.hdr->status, st);
 }
 
 int ubs_scene_backward(int32_t dim, int64_t N, const float *xyz, const float *mean,
@@ -759,15 +768,13 @@ int ubs_scene_backward(int32_t dim, int64_t N, const float *xyz, const float *me
                          w.bytes);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int64_t CN = (int64_t)C * N;
-    float *v_m2 = w.grads, *v_cn = v_m2 + CN * 2, *v_col = v_cn + CN * 3, *v_op = v_col + CN * 3,
-          *v_be = v_op + CN;
-    if (cudaMemsetAsync(w.grads, 0, CN * 10 * 4, st) != cudaSuccess)
+    if (cudaMemsetAsync(w.grads, 0, CN * kGradRow * 4, st) != cudaSuccess)
         return check_launch("scene_backward memset");
     if (int e = scene_blend(0, C, CN, n_buckets, tile_size, w.offsets, w.order, &w.hdr->total,
                             capacity, w.keys, w.recs, w.cols_n, backgrounds, tile_base,
                             view_dims, pix_base,
                             nullptr, nullptr, nullptr, render_alphas, last_ids, v_render_colors,
-                            v_render_alphas, v_m2, v_cn, v_col, v_op, v_be, &w.hdr->status, st))
+                            v_render_alphas, w.grads, &w.hdr->status, st))
         return e;
     if (CN == 0) return UBS_OK;
     if (C > 1) {
@@ -785,11 +792,7 @@ int ubs_scene_backward(int32_t dim, int64_t N, const float *xyz, const float *me
     a.depth = w.depth;
     a.status = &w.hdr->status;
     a.act = w.act; // left by the forward
-    a.v_m2 = v_m2;
-    a.v_cn = v_cn;
-    a.v_col = v_col;
-    a.v_op = v_op;
-    a.v_be = v_be;
+    a.v_rows = w.grads;
     a.g_xyz = v_xyz;
     a.g_mean = v_mean;
     a.g_scale = v_scale;

@@ -104,76 +104,41 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
 }
 
 // -------------------------------------------------- warp transpose-reduce
-// Sums 16 per-lane values over the 32 lanes of a warp with 16 shuffles
-// (instead of 16 x 5).  On return lane L holds the warp total of value
-// index ((L>>4)&1)*8 + ((L>>3)&1)*4 + ((L>>2)&1)*2 + ((L>>1)&1) in v[0];
-// lanes L and L^1 hold the same total.
-__device__ __forceinline__ int transpose_reduce_index(int lane) {
-    return ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 +
-           ((lane >> 1) & 1);
-}
-__device__ __forceinline__ float warp_transpose_reduce16(float (&v)[16], int lane) {
-    const unsigned full = 0xffffffffu;
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        const bool hi = lane & 16;
-        const float send = hi ? v[i] : v[i + 8];
-        const float keep = hi ? v[i + 8] : v[i];
-        v[i] = keep + __shfl_xor_sync(full, send, 16);
-    }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const bool hi = lane & 8;
-        const float send = hi ? v[i] : v[i + 4];
-        const float keep = hi ? v[i + 4] : v[i];
-        v[i] = keep + __shfl_xor_sync(full, send, 8);
-    }
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-        const bool hi = lane & 4;
-        const float send = hi ? v[i] : v[i + 2];
-        const float keep = hi ? v[i + 2] : v[i];
-        v[i] = keep + __shfl_xor_sync(full, send, 4);
-    }
-    {
-        const bool hi = lane & 2;
-        const float send = hi ? v[0] : v[1];
-        const float keep = hi ? v[1] : v[0];
-        v[0] = keep + __shfl_xor_sync(full, send, 2);
-    }
-    v[0] += __shfl_xor_sync(full, v[0], 1);
-    return v[0];
-}
-
 // Generalised transpose reduction of S = 2^m values (1 <= S <= 32) over the 32
 // lanes: m halving steps (each lane keeps half of its slots and adds its
 // partner's other half) then 5 - m plain butterfly steps.  Lane L returns the
-// warp total of value tr_index<S>(L); lanes with L % (32 / S) == 0 hold each
-// value exactly once.
+// warp total of value tr_index<S>(L): the 32 / S lanes that differ from L only
+// in their low 5 - m bits hold the same total, and lanes with L % (32 / S) == 0
+// hold each value exactly once.
 template <int S> __device__ __forceinline__ int tr_index(int lane) {
-    int idx = 0, n = S, h = 16;
-#pragma unroll
-    for (int step = 0; step < 5; ++step) {
-        if (n > 1) {
-            if (lane & h) idx += n / 2;
-            n >>= 1;
-            h >>= 1;
-        }
-    }
-    return idx;
+    return (int)((unsigned)lane / (32u / S)); // lane bits 4 .. 5 - log2 S
 }
-template <int S> __device__ __forceinline__ float tr_reduce(float (&v)[S], int lane) {
+// Lane-bit masks of the transpose reductions: m[j] is all ones when bit
+// 4 - j of the lane index is set.  Each exchange of tr_reduce picks the value
+// to send and the one to keep with bitwise selects on these masks, which
+// needs no predicate registers.
+struct LaneMasks {
+    uint32_t m[5];
+};
+__device__ __forceinline__ LaneMasks lane_masks(int lane) {
+    LaneMasks l;
+#pragma unroll
+    for (int j = 0; j < 5; ++j) l.m[j] = (lane & (16 >> j)) ? ~0u : 0u;
+    return l;
+}
+template <int S> __device__ __forceinline__ float tr_reduce(float (&v)[S], const LaneMasks &lm) {
     const unsigned full = 0xffffffffu;
     int n = S, h = 16;
 #pragma unroll
     for (int step = 0; step < 5; ++step) {
         if (n > 1) {
-            const bool hi = lane & h;
+            const uint32_t m = lm.m[step];
 #pragma unroll
             for (int i = 0; i < S / 2; ++i) {
                 if (i < n / 2) {
-                    const float send = hi ? v[i] : v[i + n / 2];
-                    const float keep = hi ? v[i + n / 2] : v[i];
+                    const uint32_t a = __float_as_uint(v[i]), b = __float_as_uint(v[i + n / 2]);
+                    const float send = __uint_as_float((a & m) | (b & ~m));
+                    const float keep = __uint_as_float((b & m) | (a & ~m));
                     v[i] = keep + __shfl_xor_sync(full, send, h);
                 }
             }
