@@ -42,14 +42,16 @@ int scene_blend(int fwd, int32_t C, int64_t CN, int32_t n_buckets, int32_t tile_
                 cudaStream_t st);
 
 // scene_act.cu (compiled with IEEE math): activated scales, betas and
-// opacities, act = [N, D] | [N, D - 2] | [N]
+// opacities, act = [N, D] | [N, D - 2] | [N] at the 16-byte aligned section
+// offsets 0, act_beta_off, act_opac_off
 int launch_scene_act(int64_t N, int D, const float *scale, const float *beta, const float *opac,
                      float *act, cudaStream_t st);
 
 namespace {
 
 constexpr int kTileMaxViews = 1 << 16;
-// floats per primitive of the activation section (D + D - 2 + 1, D <= 7)
+// floats per primitive of the activation section (D + D - 2 + 1, D <= 7),
+// plus up to 8 floats of section alignment
 constexpr int kActPerPrim = 13;
 // floats per gradient row of the backward blend (GRAD_ROW in raster.cu)
 constexpr int kGradRow = 12;
@@ -77,6 +79,7 @@ struct SceneArgs {
     const int32_t *dims, *tile_base;
     float tile_size, eps2d, near_p, far_p, radius_clip;
     const float *act;         // activated scale [N,D] | beta [N,D-2] | opacity [N]
+    const float *act_b, *act_o; // its beta and opacity sections (act_beta_off, act_opac_off)
     const uint8_t *prim_mask; // optional: primitives with 0 are not rendered
     int color_mode;           // 0: rgb; 1: depth in channel 0 (one view, forward only)
     // outputs / workspace
@@ -176,7 +179,7 @@ template <int D>
 __device__ __forceinline__ bool prim_rows(const SceneArgs &a, int64_t idx, int64_t n, int lane,
                                           float *stage, PrimRows &r) {
     constexpr int K = D - 3, NL = D * (D - 1) / 2;
-    const float *act_s = a.act, *act_b = a.act + a.N * D, *act_o = act_b + a.N * (D - 2);
+    const float *act_s = a.act, *act_b = a.act_b, *act_o = a.act_o;
     const int64_t w0 = idx - lane, n0 = n - lane;
     const bool staged = w0 + 32 <= (int64_t)a.C * a.N && n0 >= 0 && n0 + 32 <= a.N;
     if (__all_sync(0xffffffffu, staged)) {
@@ -269,8 +272,6 @@ __global__ void __launch_bounds__(PRIM_THREADS, D == 6 ? 8 : 6) scene_prim_fwd_k
     PrimRows rows;
     if (prim_rows<D>(a, idx, n, lane, stage[threadIdx.x >> 5], rows)) __syncwarp();
     if (idx >= (int64_t)a.C * a.N) return;
-    const float4 *vrow = reinterpret_cast<const float4 *>(a.v_rows + idx * kGradRow);
-    const float4 vr0 = vrow[0], vr1 = vrow[1], vr2 = vrow[2];
     PrimFwd<D> f;
     prim_forward<D>(a, rows, v, f);
     const Cam cam = view_cam(a, v);
@@ -541,7 +542,7 @@ SceneWs scene_ws(void *base, int32_t C, int64_t N, int32_t nb, int64_t cap) {
     w.scratch = reinterpret_cast<uint64_t *>(take(cap * 8));
     w.cols_n = reinterpret_cast<float4 *>(take((size_t)N * 16));
     w.grads = reinterpret_cast<float *>(take(CN * kGradRow * 4));
-    w.act = reinterpret_cast<float *>(take((size_t)N * kActPerPrim * 4));
+    w.act = reinterpret_cast<float *>(take(((size_t)N * kActPerPrim + 8) * 4));
     w.bytes = o;
     return w;
 }
@@ -686,6 +687,8 @@ int ubs_scene_forward_masked(int32_t dim, int64_t N, const float *xyz, const flo
     a.bucket_counts = w.bucket_counts;
     a.status = &w.hdr->status;
     a.act = w.act;
+    a.act_b = w.act + act_beta_off(N, dim);
+    a.act_o = w.act + act_opac_off(N, dim);
     if (CN > 0) {
         if (int e = launch_scene_act(N, dim, scale, beta, opacity, w.act, st)) return e;
         UBS_TIMED("scene_prim_fwd", st,
@@ -792,6 +795,8 @@ int ubs_scene_backward(int32_t dim, int64_t N, const float *xyz, const float *me
     a.depth = w.depth;
     a.status = &w.hdr->status;
     a.act = w.act; // left by the forward
+    a.act_b = w.act + act_beta_off(N, dim);
+    a.act_o = w.act + act_opac_off(N, dim);
     a.v_rows = w.grads;
     a.g_xyz = v_xyz;
     a.g_mean = v_mean;

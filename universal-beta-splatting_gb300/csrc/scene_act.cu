@@ -59,12 +59,13 @@ __global__ void scene_act_kernel(int64_t N, int D, const float *__restrict__ sca
                                  float *__restrict__ act, int vec) {
     const int64_t ns = N * D, nb = N * (D - 2);
     const int64_t qs = (ns + 3) / 4, qb = (nb + 3) / 4, qo = (N + 3) / 4;
+    float *act_b = act + act_beta_off(N, D), *act_o = act + act_opac_off(N, D);
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < qs + qb + qo;
          q += stride) {
         if (q < qs) act_quad<0>(scale, act, q, ns, vec & 1);
-        else if (q < qs + qb) act_quad<1>(beta, act + ns, q - qs, nb, vec & 2);
-        else act_quad<2>(opac, act + ns + nb, q - qs - qb, N, vec & 4);
+        else if (q < qs + qb) act_quad<1>(beta, act_b, q - qs, nb, vec & 2);
+        else act_quad<2>(opac, act_o, q - qs - qb, N, vec & 4);
     }
 }
 
@@ -75,8 +76,9 @@ int launch_scene_act(int64_t N, int D, const float *scale, const float *beta, co
     if (N == 0) return UBS_OK;
     const int64_t ns = N * D, nb = N * (D - 2);
     auto a16 = [](const void *p) { return ((uintptr_t)p & 15) == 0; };
-    const int vec = (a16(scale) && a16(act) ? 1 : 0) | (a16(beta) && a16(act + ns) ? 2 : 0) |
-                    (a16(opac) && a16(act + ns + nb) ? 4 : 0);
+    const int vec = (a16(scale) && a16(act) ? 1 : 0) |
+                    (a16(beta) && a16(act + act_beta_off(N, D)) ? 2 : 0) |
+                    (a16(opac) && a16(act + act_opac_off(N, D)) ? 4 : 0);
     const int64_t quads = (ns + 3) / 4 + (nb + 3) / 4 + (N + 3) / 4;
     int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) == cudaSuccess)

@@ -352,17 +352,54 @@ static __global__ void __launch_bounds__(1024) bucket_scan_order_kernel(
 
 // Bitonic sort of the 32 * E keys of a warp held E per lane in registers,
 // blocked (element i = lane * E + e): exchange distances below E stay inside
-// a lane, larger ones are lane-xor shuffles.  Only the loop over a lane's E
-// elements is unrolled (so the key arrays stay in registers); the stage loops
-// run at run time, with one unrolled body per in-lane distance, which keeps
-// the code small enough for the instruction cache.
-template <int E, int J>
-__device__ __forceinline__ void bitonic_in_lane(uint64_t (&v)[E], int lane, int k) {
+// a lane, larger ones are lane-xor shuffles.  The network runs in two phases
+// so that no compare-exchange recomputes its direction:
+//   * stages k < E sort runs inside a lane: distances and directions are
+//     compile-time (element e of a run of k ascends when e & k == 0);
+//   * stages k >= E: the direction of all E elements of a lane is the same,
+//     ((lane * E) & k) == 0, one predicate per stage; the stage loop runs at
+//     run time with one unrolled body per in-lane distance, which keeps the
+//     code small enough for the instruction cache.
+// The network is the same as the textbook bitonic sort, so the result is.
+template <int E, int J, int K>
+__device__ __forceinline__ void bitonic_run_pass(uint64_t (&v)[E]) {
 #pragma unroll
     for (int e = 0; e < E; ++e) {
         const int p = e ^ J;
         if (p > e) {
-            const bool up = (((lane * E + e) & k) == 0);
+            const uint64_t a = v[e], b = v[p];
+            const bool sw = ((e & K) == 0) ? (a > b) : (a < b);
+            v[e] = sw ? b : a;
+            v[p] = sw ? a : b;
+        }
+    }
+}
+template <int E, int K, int J> struct BitonicRunStage {
+    static __device__ __forceinline__ void run(uint64_t (&v)[E]) {
+        bitonic_run_pass<E, J, K>(v);
+        BitonicRunStage<E, K, J / 2>::run(v);
+    }
+};
+template <int E, int K> struct BitonicRunStage<E, K, 0> {
+    static __device__ __forceinline__ void run(uint64_t (&)[E]) {}
+};
+template <int E, int K> struct BitonicRuns { // stages K, 2K, .. < E
+    static __device__ __forceinline__ void run(uint64_t (&v)[E]) {
+        BitonicRunStage<E, K, K / 2>::run(v);
+        BitonicRuns<E, (2 * K < E ? 2 * K : 0)>::run(v);
+    }
+};
+template <int E> struct BitonicRuns<E, 0> {
+    static __device__ __forceinline__ void run(uint64_t (&)[E]) {}
+};
+
+// One in-lane pass of distance J with the lane's direction `up`.
+template <int E, int J>
+__device__ __forceinline__ void bitonic_in_lane(uint64_t (&v)[E], bool up) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int p = e ^ J;
+        if (p > e) {
             const uint64_t a = v[e], b = v[p];
             const bool sw = (a > b) == up;
             v[e] = sw ? b : a;
@@ -374,28 +411,26 @@ __device__ __forceinline__ void bitonic_in_lane(uint64_t (&v)[E], int lane, int 
 template <int E>
 __device__ __forceinline__ void warp_bitonic(uint64_t (&v)[E], int lane) {
     constexpr int N = 32 * E;
+    BitonicRuns<E, (E >= 4 ? 2 : 0)>::run(v); // k = 2 .. E / 2 inside the lane
 #pragma unroll 1
-    for (int k = 2; k <= N; k <<= 1) {
+    for (int k = E >= 2 ? E : 2; k <= N; k <<= 1) {
+        const bool up = ((lane * E) & k) == 0;
 #pragma unroll 1
         for (int j = k >> 1; j >= E; j >>= 1) { // across lanes
             const int lj = j / E;
-            const bool lower = (lane & lj) == 0;
+            const bool keep_min = ((lane & lj) == 0) == up;
 #pragma unroll
             for (int e = 0; e < E; ++e) {
                 const uint64_t o = __shfl_xor_sync(0xffffffffu, v[e], lj);
-                const bool up = (((lane * E + e) & k) == 0);
-                const bool keep_min = lower == up;
-                const bool o_less = o < v[e];
-                v[e] = (keep_min == o_less) ? o : v[e];
+                v[e] = (keep_min == (o < v[e])) ? o : v[e];
             }
         }
-        // inside a lane: distances min(k / 2, E / 2) .. 1
-        const int jmax = (k >> 1) < E ? (k >> 1) : (E >> 1);
-        if (E >= 32 && jmax >= 16) bitonic_in_lane<E, (E >= 32 ? 16 : 1)>(v, lane, k);
-        if (E >= 16 && jmax >= 8) bitonic_in_lane<E, (E >= 16 ? 8 : 1)>(v, lane, k);
-        if (E >= 8 && jmax >= 4) bitonic_in_lane<E, (E >= 8 ? 4 : 1)>(v, lane, k);
-        if (E >= 4 && jmax >= 2) bitonic_in_lane<E, (E >= 4 ? 2 : 1)>(v, lane, k);
-        if (E >= 2 && jmax >= 1) bitonic_in_lane<E, 1>(v, lane, k);
+        // inside a lane: distances E / 2 .. 1
+        if (E >= 32) bitonic_in_lane<E, (E >= 32 ? 16 : 1)>(v, up);
+        if (E >= 16) bitonic_in_lane<E, (E >= 16 ? 8 : 1)>(v, up);
+        if (E >= 8) bitonic_in_lane<E, (E >= 8 ? 4 : 1)>(v, up);
+        if (E >= 4) bitonic_in_lane<E, (E >= 4 ? 2 : 1)>(v, up);
+        if (E >= 2) bitonic_in_lane<E, 1>(v, up);
     }
 }
 
@@ -421,7 +456,7 @@ __device__ __forceinline__ void warp_sort_bucket(const uint64_t *__restrict__ ke
 // buckets go to the device-side lists: mid (<= SMALL_SEG) from the front of
 // `lists`, big from the back.  counters = {n_big, n_mid}.
 template <typename Writer>
-__global__ void __launch_bounds__(256) bucket_sort_warp_kernel(
+__global__ void __launch_bounds__(256, 3) bucket_sort_warp_kernel(
     int64_t n_buckets, const int32_t *__restrict__ offsets, const int64_t *T_dev, int64_t cap,
     const uint64_t *__restrict__ keys, int32_t *lists, int32_t *counters, Writer w) {
     const int lane = threadIdx.x & 31;

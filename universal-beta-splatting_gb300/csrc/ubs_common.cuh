@@ -55,6 +55,17 @@ __device__ __forceinline__ float clamp01_eps(float x) {
     return x > maxv ? maxv : x;
 }
 
+// ------------------------------------------ scene activation sections
+// Float offsets of the activated-parameter sections of the fused scene
+// workspace: scales [N, D] at 0, betas [N, D - 2] and opacities [N] each on a
+// 16-byte boundary (so that rows of 32 primitives can be bulk-copied).
+__host__ __device__ inline int64_t act_beta_off(int64_t N, int D) {
+    return (N * D + 3) & ~int64_t(3);
+}
+__host__ __device__ inline int64_t act_opac_off(int64_t N, int D) {
+    return act_beta_off(N, D) + ((N * (D - 2) + 3) & ~int64_t(3));
+}
+
 // ------------------------------------------ mbarrier + bulk async copy (TMA)
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
