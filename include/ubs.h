@@ -538,12 +538,15 @@ int ubs_scene_stats(const void *workspace, int64_t *n_isects, uint32_t *status, 
 
 /* Occupancy variant of the blend kernels (no reference counterpart; the
  * reference's launch shape is fixed, rasterize_to_pixels_fwd.cu:269-292):
- * for 3 channels and tiles of at most 16 x 16 pixels, each variant trades
- * records per staged batch against CTAs per SM --
+ * for 3 channels and tiles of at most 16 x 16 pixels the forward's variants
+ * trade records per staged batch against CTAs per SM, the backward's the
+ * register bound and the way a batch's per-record sums are accumulated --
  *   forward:  0 (default): 256-record batches, 8 CTAs per SM;
  *             1: 128-record batches, 10 CTAs per SM; 2: 256-record, 6 CTAs per SM
- *   backward: 0 (default): 128-record batches, 8 CTAs per SM;
- *             1: 256-record batches, 6 CTAs per SM; 2: 128-record, 6 CTAs per SM
+ *   backward: 0 (default): 128-record batches, 8 CTAs per SM, per-warp lists
+ *             of reduced sums written with plain stores;
+ *             1: the same at 7 CTAs per SM; 2: 128-record batches, 8 CTAs per
+ *             SM, one shared accumulator row per record (shared atomics)
  * (for 16 x 16 tiles; an 8 x 8 tile's batches are a quarter of that).
  * Process-wide: it applies to every later launch from any thread (an
  * autotuner sets it between measured steps, outside stream capture).  Images

@@ -6,9 +6,10 @@ pixels is one CTA of TS*TS/2 threads (two pixels each), its batch of staged
 records is TS*TS entries, and with the shared memory that batch needs it
 fixes how many CTAs fit on an SM.  It also changes the intersection count
 (smaller tiles: more buckets, fewer wasted pixels per record).  For tiles up
-to 16 x 16 the blend kernels are compiled in occupancy variants
-(ubs_set_blend_variant: records per staged batch against CTAs per SM, for the
-forward and the backward separately).  Which point is fastest depends on the
+to 16 x 16 the blend kernels are compiled in variants (ubs_set_blend_variant,
+for the forward and the backward separately: the forward's trade records per
+staged batch against CTAs per SM, the backward's its register bound and how a
+batch's per-record gradient sums are accumulated).  Which point is fastest depends on the
 resolution mix and the scene's footprint sizes, so it is measured: each
 candidate runs the caller's step a few times after a warm-up, timed with CUDA
 events on the launching stream, and the winner is cached under a
