@@ -297,6 +297,46 @@ def test_blend_fwd_bwd(C, N, W, H, ts, channels, bg):
         np.testing.assert_allclose(npy(bg_dev.grad), npy(v_bg), rtol=1e-4, atol=1e-3)
 
 
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_blend_bwd_row_list_overflow(variant):
+    # Wide, faint splats: every record of a tile covers every warp's 8 x 8 box
+    # and no pixel terminates, so each warp visits all 128 records of every
+    # backward batch.  Variants 0 and 1 keep the reduced sums of 64 visits per
+    # warp and batch in their row lists and add the rest straight to the
+    # gradient arrays; variant 2 accumulates through shared atomics.  All three
+    # must give the FP64 oracle's gradients.
+    from gsplat.cuda._wrapper import rasterize_to_pixels
+    from ubs.autotune import get_blend_variant, set_blend_variant
+    N, W, H, ts = 1200, 64, 48, 16
+    s, colors, offs, fl = _blend_inputs(N, W, H, 1, seed=5, ts=ts, big_frac=1.0)
+    s["opacities"] = s["opacities"] * 0.01
+    counts = np.diff(np.append(npy(offs).reshape(-1), fl.numel()))
+    assert counts.min() > 4 * 128  # several full batches per tile
+    ts_in = [s["means2d"], s["conics"], colors, s["opacities"], s["betas"]]
+    ts_dev = [t.to(DEV).requires_grad_(True) for t in ts_in]
+    g = torch.Generator().manual_seed(3)
+    old = get_blend_variant()
+    set_blend_variant(0, variant)
+    try:
+        rc, ra = rasterize_to_pixels(*ts_dev, W, H, ts, offs, fl)
+        wc = torch.randn(rc.shape, generator=g)
+        wa = torch.randn(ra.shape, generator=g)
+        ((rc * wc.to(DEV)).sum() + (ra * wa.to(DEV)).sum()).backward()
+        torch.cuda.synchronize()
+    finally:
+        set_blend_variant(*old)
+    np64 = [npy(t).astype(np.float64) for t in ts_in]
+    _, oa64, li64 = orc.rasterize_to_pixels(*np64, W, H, ts, npy(offs), npy(fl),
+                                            dtype=np.float64)
+    assert float(oa64.min()) > 0.5 and int(li64.min()) > 0  # no pixel terminated early...
+    assert float(oa64.max()) < 1 - 1e-4
+    ref = orc.rasterize_to_pixels_bwd(*np64, W, H, ts, npy(offs), npy(fl), oa64, li64,
+                                      npy(wc).astype(np.float64), npy(wa).astype(np.float64),
+                                      dtype=np.float64)
+    for t, r, nm in zip(ts_dev, ref, ("v_means2d", "v_conics", "v_colors", "v_opac", "v_betas")):
+        grad_close(npy(t.grad), r, nm, rel_l2=1e-3)
+
+
 def test_blend_termination_and_masks():
     """Opaque scene: early termination (T <= 1e-4), the 0.999 clamp and tile masks."""
     from gsplat.cuda._wrapper import rasterize_to_pixels
