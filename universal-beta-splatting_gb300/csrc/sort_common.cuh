@@ -15,6 +15,7 @@ constexpr int SMALL_SEG = 4096; // longest bucket sorted by one CTA in shared me
 constexpr int SORT_THREADS = 256;
 constexpr int BIG_THREADS = 1024;
 constexpr int MERGE_ITEMS = 8;
+constexpr int EMIT_ROUNDS = 4; // (entry, tile) rounds of 32 whose cursor atomics overlap
 
 __host__ __device__ __forceinline__ int64_t imin64(int64_t a, int64_t b) { return a < b ? a : b; }
 
@@ -201,24 +202,24 @@ __device__ __forceinline__ void warp_emit_rects(uint32_t n, uint32_t bw, uint32_
         const uint32_t ry = local / o_bw, rx = local - ry * o_bw;
         slot = o_cur + (int64_t)ry * o_pitch + rx;
     };
-    // two rounds per iteration: both rounds' cursor atomics are in flight
-    // before either round stores its keys
-    for (uint32_t base = 0; base < total; base += 64) {
-        const uint32_t j0 = base + lane, j1 = base + 32 + lane;
-        int32_t *s0, *s1;
-        uint64_t k0, k1;
-        locate(j0, s0, k0);
-        const bool two = base + 32 < total; // warp-uniform
-        if (two) locate(j1, s1, k1);
-        const int32_t p0 = j0 < total ? atomicAdd(s0, 1) : -1;
-        const int32_t p1 = (two && j1 < total) ? atomicAdd(s1, 1) : -1;
-        if (j0 < total) {
-            if (p0 >= 0 && p0 < cap) keys[p0] = k0;
-            else atomicOr(status, DEV_ERR_OVERFLOW);
-        }
-        if (two && j1 < total) {
-            if (p1 >= 0 && p1 < cap) keys[p1] = k1;
-            else atomicOr(status, DEV_ERR_OVERFLOW);
+    // EMIT_ROUNDS rounds per iteration: all their cursor atomics are in
+    // flight before any of them stores its key
+    for (uint32_t base = 0; base < total; base += 32 * EMIT_ROUNDS) {
+        int32_t *sl[EMIT_ROUNDS];
+        uint64_t kk[EMIT_ROUNDS];
+        int32_t pos[EMIT_ROUNDS];
+#pragma unroll
+        for (int r = 0; r < EMIT_ROUNDS; ++r)
+            if (base + 32 * r < total) locate(base + 32 * r + lane, sl[r], kk[r]); // uniform
+#pragma unroll
+        for (int r = 0; r < EMIT_ROUNDS; ++r)
+            pos[r] = base + 32 * r + lane < total ? atomicAdd(sl[r], 1) : -1;
+#pragma unroll
+        for (int r = 0; r < EMIT_ROUNDS; ++r) {
+            if (base + 32 * r + lane < total) {
+                if (pos[r] >= 0 && pos[r] < cap) keys[pos[r]] = kk[r];
+                else atomicOr(status, DEV_ERR_OVERFLOW);
+            }
         }
     }
 }
