@@ -135,6 +135,32 @@ def test_fused_many_tiles_match_dropin():
     assert float(alphas.max()) > 0.5
 
 
+def test_fused_more_buckets_than_one_scan_cta():
+    # 9 views of 1920x1080 at 16x16 tiles: 73,440 (view, tile) buckets, more
+    # than the one-CTA scan takes, so the replicated bucket counters are
+    # folded, scanned device-wide and turned into replica cursors by separate
+    # kernels and the launch order comes from the order kernel
+    p = make_params(3000, 6, seed=37)
+    cams = [S.orbit_view(60 + v, 3.0, 1920, 1080, 1500.0, 1500.0, device=DEV) for v in range(9)]
+    bgs = torch.rand(9, 3, generator=torch.Generator().manual_seed(4)).to(DEV)
+    _, views, colors, alphas, leaves = fused_render(p, cams, bgs)
+    assert views.n_buckets > 65536
+    imgs = views.split(colors)
+    g = torch.Generator().manual_seed(5)
+    wts = [torch.rand(imgs[v].shape, generator=g).to(DEV) for v in range(9)]
+    sum((imgs[v] * wts[v]).sum() for v in range(9)).backward()
+    grads = {k: torch.zeros_like(v) for k, v in p.items()}
+    for v, cam in enumerate(cams):
+        img_d, _, leaves_d = dropin_render(p, cam, bgs[v])
+        assert float((imgs[v] - img_d).detach().abs().max()) < 1e-5, v
+        (img_d * wts[v]).sum().backward()
+        for k in grads:
+            grads[k] += leaves_d[k].grad
+    for k in grads:
+        assert rel_l2(leaves[k].grad, grads[k]) < 1e-4, (k, rel_l2(leaves[k].grad, grads[k]))
+    assert float(alphas.max()) > 0.5
+
+
 def test_fused_capacity_overflow_is_recovered():
     p = make_params(4000, 6, seed=21)
     cam = S.orbit_view(7, 3.0, 256, 192, 220.0, 220.0, device=DEV)

@@ -50,6 +50,12 @@ int launch_scene_act(int64_t N, int D, const float *scale, const float *beta, co
 namespace {
 
 constexpr int kTileMaxViews = 1 << 16;
+// Replicas of the per-bucket intersection counters and cursors: entry idx
+// counts and emits through replica idx % kCountReplicas, which spreads a
+// bucket's atomics over that many L2 lines (a 1080p frame has about 520
+// intersections per bucket).  A bucket's keys stay one contiguous range: the
+// replicas own consecutive sub-ranges of it.
+constexpr int kCountReplicas = 8;
 // floats per primitive of the activation section (D + D - 2 + 1, D <= 7),
 // plus up to 8 floats of section alignment
 constexpr int kActPerPrim = 13;
@@ -87,7 +93,8 @@ struct SceneArgs {
     float4 *cols_n; // colour row per primitive (written by the view-0 entries)
     int32_t *radius;
     float *depth;
-    int32_t *bucket_counts;
+    int32_t *bucket_counts; // [kCountReplicas][n_buckets]
+    int32_t n_buckets;
     uint32_t *status;
     // backward
     // gradient row per (view, primitive) entry from the backward blend:
@@ -321,7 +328,7 @@ __global__ void __launch_bounds__(PRIM_THREADS, D == 6 ? 8 : 6) scene_prim_fwd_k
     const uint32_t y1 = min(max(0u, __float2uint_rz(ceilf(ty + rr))), TH);
     if (x1 <= x0 || y1 <= y0) return;
     if (__float_as_int(p.depth) < 0) atomicOr(a.status, DEV_ERR_NEG_DEPTH);
-    int32_t *bc = a.bucket_counts + a.tile_base[v];
+    int32_t *bc = a.bucket_counts + (int64_t)(idx % kCountReplicas) * a.n_buckets + a.tile_base[v];
     for (uint32_t y = y0; y < y1; ++y)
         for (uint32_t x = x0; x < x1; ++x) atomicAdd(&bc[y * TW + x], 1);
 }
@@ -335,7 +342,7 @@ __global__ void scene_emit_kernel(int64_t CN, int64_t N, const Rec *__restrict__
                                   const int32_t *__restrict__ radius,
                                   const float *__restrict__ depth,
                                   const int32_t *__restrict__ dims,
-                                  const int32_t *__restrict__ tile_base, float ts,
+                                  const int32_t *__restrict__ tile_base, int32_t nb, float ts,
                                   int32_t *__restrict__ cursor, uint64_t *__restrict__ keys,
                                   int64_t cap, uint32_t *status) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -355,7 +362,7 @@ __global__ void scene_emit_kernel(int64_t CN, int64_t N, const Rec *__restrict__
         if (x1 > x0 && y1 > y0) {
             bw = x1 - x0;
             n = bw * (y1 - y0);
-            cur = cursor + tile_base[v] + (int64_t)y0 * TW + x0;
+            cur = cursor + (idx % kCountReplicas) * nb + tile_base[v] + (int64_t)y0 * TW + x0;
             key = ((uint64_t)(uint32_t)__float_as_int(depth[idx]) << 32) | (uint64_t)idx;
             pitch = TW;
         }
@@ -509,7 +516,7 @@ struct SceneWs {
     Rec *recs;
     int32_t *radius;
     float *depth;
-    int32_t *bucket_counts, *offsets, *cursor, *big_list, *order;
+    int32_t *bucket_counts, *offsets, *cursor, *big_list, *order, *totals;
     int64_t *block_sums;
     uint64_t *keys, *scratch;
     float4 *cols_n;
@@ -532,9 +539,10 @@ SceneWs scene_ws(void *base, int32_t C, int64_t N, int32_t nb, int64_t cap) {
     w.recs = reinterpret_cast<Rec *>(take(CN * sizeof(Rec)));
     w.radius = reinterpret_cast<int32_t *>(take(CN * 4));
     w.depth = reinterpret_cast<float *>(take(CN * 4));
-    w.bucket_counts = reinterpret_cast<int32_t *>(take((size_t)nb * 4));
+    w.bucket_counts = reinterpret_cast<int32_t *>(take((size_t)nb * kCountReplicas * 4));
     w.offsets = reinterpret_cast<int32_t *>(take((size_t)(nb + 1) * 4));
-    w.cursor = reinterpret_cast<int32_t *>(take((size_t)nb * 4));
+    w.cursor = reinterpret_cast<int32_t *>(take((size_t)nb * kCountReplicas * 4));
+    w.totals = reinterpret_cast<int32_t *>(take((size_t)nb * 4));
     w.big_list = reinterpret_cast<int32_t *>(take((size_t)nb * 4));
     w.order = reinterpret_cast<int32_t *>(take((size_t)nb * 4));
     w.block_sums = reinterpret_cast<int64_t *>(take(((nb + SCAN_TILE - 1) / SCAN_TILE + 1) * 8));
@@ -678,13 +686,15 @@ int ubs_scene_forward_masked(int32_t dim, int64_t N, const float *xyz, const flo
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int64_t CN = (int64_t)C * N;
     if (cudaMemsetAsync(w.hdr, 0, sizeof(SceneHeader), st) != cudaSuccess ||
-        cudaMemsetAsync(w.bucket_counts, 0, (size_t)n_buckets * 4, st) != cudaSuccess)
+        cudaMemsetAsync(w.bucket_counts, 0, (size_t)n_buckets * kCountReplicas * 4, st) !=
+            cudaSuccess)
         return check_launch("scene_forward memset");
     a.recs = w.recs;
     a.cols_n = w.cols_n;
     a.radius = w.radius;
     a.depth = w.depth;
     a.bucket_counts = w.bucket_counts;
+    a.n_buckets = n_buckets;
     a.status = &w.hdr->status;
     a.act = w.act;
     a.act_b = w.act + act_beta_off(N, dim);
@@ -702,22 +712,31 @@ int ubs_scene_forward_masked(int32_t dim, int64_t N, const float *xyz, const flo
     const bool one_cta = n_buckets <= SCAN_ORDER_MAX;
     if (one_cta) {
         UBS_TIMED("bucket_scan_order", st,
-                  bucket_scan_order_kernel<<<1, 1024, 0, st>>>(w.bucket_counts, n_buckets,
-                                                               w.offsets, &w.hdr->total, w.order));
+                  bucket_scan_order_kernel<kCountReplicas><<<1, 1024, 0, st>>>(
+                      w.bucket_counts, n_buckets, w.offsets, &w.hdr->total, w.order, w.cursor,
+                      w.totals));
         note_launch();
         if (int e = check_launch("bucket_scan_order")) return e;
-    } else if (int e = device_exclusive_scan<int32_t>(w.bucket_counts, w.offsets, n_buckets,
-                                                      w.block_sums, &w.hdr->total, st)) {
-        return e;
+    } else {
+        UBS_TIMED("fold_replicas", st,
+                  fold_replicas_kernel<kCountReplicas><<<grid_for(n_buckets, 256), 256, 0, st>>>(
+                      w.bucket_counts, n_buckets, w.totals));
+        note_launch();
+        if (int e = check_launch("fold_replicas")) return e;
+        if (int e = device_exclusive_scan<int32_t>(w.totals, w.offsets, n_buckets, w.block_sums,
+                                                   &w.hdr->total, st))
+            return e;
+        UBS_TIMED("replica_cursors", st,
+                  replica_cursors_kernel<kCountReplicas><<<grid_for(n_buckets, 256), 256, 0, st>>>(
+                      w.bucket_counts, n_buckets, w.offsets, w.cursor));
+        note_launch();
+        if (int e = check_launch("replica_cursors")) return e;
     }
-    if (cudaMemcpyAsync(w.cursor, w.offsets, (size_t)n_buckets * 4, cudaMemcpyDeviceToDevice, st) !=
-        cudaSuccess)
-        return check_launch("scene cursor copy");
     if (CN > 0) {
         UBS_TIMED("scene_emit", st,
                   scene_emit_kernel<<<grid_for(CN, 256), 256, 0, st>>>(
-                      CN, N, w.recs, w.radius, w.depth, view_dims, tile_base, (float)tile_size,
-                      w.cursor, w.keys, capacity, &w.hdr->status));
+                      CN, N, w.recs, w.radius, w.depth, view_dims, tile_base, n_buckets,
+                      (float)tile_size, w.cursor, w.keys, capacity, &w.hdr->status));
         note_launch();
         if (int e = check_launch("scene_emit")) return e;
     }

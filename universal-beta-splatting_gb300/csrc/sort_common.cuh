@@ -279,9 +279,17 @@ static __global__ void __launch_bounds__(1024) bucket_order_kernel(const int32_t
 // bucket order of bucket_order_kernel (a counting sort by record count).
 // Each of the 1024 threads scans a contiguous run of buckets.
 constexpr int SCAN_ORDER_MAX = 1024 * 64;
-static __global__ void __launch_bounds__(1024) bucket_scan_order_kernel(
+// The counts come in R replicas ([R][n], replica-major: the atomics of a
+// bucket spread over R lines).  First the CTA folds them into totals[b] (the
+// bucket's count) with consecutive threads on consecutive buckets; the scan
+// and the order work on the totals; last, cursor[r n + b] receives the start
+// of replica r's sub-range of bucket b (its bucket offset plus the counts of
+// replicas 0 .. r - 1), again on consecutive buckets.
+template <int R>
+__global__ void __launch_bounds__(1024) bucket_scan_order_kernel(
     const int32_t *__restrict__ counts, int32_t n, int32_t *__restrict__ offsets,
-    int64_t *__restrict__ total, int32_t *__restrict__ order) {
+    int64_t *__restrict__ total, int32_t *__restrict__ order, int32_t *__restrict__ cursor,
+    int32_t *__restrict__ totals) {
     __shared__ int32_t bins[ORDER_BINS];
     __shared__ int64_t wtot[32];
     __shared__ int32_t btot[32];
@@ -289,10 +297,17 @@ static __global__ void __launch_bounds__(1024) bucket_scan_order_kernel(
     const int per = (n + 1023) / 1024;
     const int b0 = min(n, tid * per), b1 = min(n, b0 + per);
     for (int i = tid; i < ORDER_BINS; i += blockDim.x) bins[i] = 0;
+    for (int b = tid; b < n; b += blockDim.x) {
+        int32_t c = 0;
+#pragma unroll
+        for (int r = 0; r < R; ++r) c += counts[(int64_t)r * n + b];
+        totals[b] = c;
+    }
     __syncthreads();
+    auto count = [&](int b) { return totals[b]; };
     int64_t run = 0;
     for (int b = b0; b < b1; ++b) {
-        const int32_t c = counts[b];
+        const int32_t c = count(b);
         run += c;
         const int64_t q = c >> 2;
         atomicAdd(&bins[ORDER_BINS - 1 - (int)(q < ORDER_BINS - 1 ? q : ORDER_BINS - 1)], 1);
@@ -319,7 +334,7 @@ static __global__ void __launch_bounds__(1024) bucket_scan_order_kernel(
     int64_t off = wtot[wid] + inc - run;
     for (int b = b0; b < b1; ++b) {
         offsets[b] = (int32_t)off;
-        off += counts[b];
+        off += count(b);
     }
     if (tid == blockDim.x - 1) *total = off;
     // heaviest-first order: exclusive scan of the bins, then a scatter
@@ -345,9 +360,43 @@ static __global__ void __launch_bounds__(1024) bucket_scan_order_kernel(
     bins[tid] = x - v + (wid ? btot[wid - 1] : 0);
     __syncthreads();
     for (int b = b0; b < b1; ++b) {
-        const int64_t q = counts[b] >> 2;
+        const int64_t q = count(b) >> 2;
         order[atomicAdd(&bins[ORDER_BINS - 1 - (int)(q < ORDER_BINS - 1 ? q : ORDER_BINS - 1)],
                         1)] = b;
+    }
+    for (int b = tid; b < n; b += blockDim.x) { // offsets written above by this CTA
+        int32_t o = offsets[b];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            cursor[(int64_t)r * n + b] = o;
+            o += counts[(int64_t)r * n + b];
+        }
+    }
+}
+
+// Larger frames (more buckets than one CTA scans): the replicas' sums ...
+template <int R>
+__global__ void fold_replicas_kernel(const int32_t *__restrict__ counts, int32_t n,
+                                     int32_t *__restrict__ totals) {
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    int32_t c = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) c += counts[(int64_t)r * n + b];
+    totals[b] = c;
+}
+// ... and, after their exclusive scan, the replicas' cursors.
+template <int R>
+__global__ void replica_cursors_kernel(const int32_t *__restrict__ counts, int32_t n,
+                                       const int32_t *__restrict__ offsets,
+                                       int32_t *__restrict__ cursor) {
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    int32_t off = offsets[b];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        cursor[(int64_t)r * n + b] = off;
+        off += counts[(int64_t)r * n + b];
     }
 }
 
