@@ -159,8 +159,8 @@ int ubs_projection_bwd(int32_t C, int64_t N, const float *means, const float *co
  * Step 2: isect_ids [n_isects] int64 (cam | tile | depth bits) and
  *   flatten_ids [n_isects] int32, sorted like the reference's stable radix sort
  *   when sort != 0, else in the reference's generation order.  Workspace:
- *   ubs_isect_sort_workspace_bytes(); it must begin with the count workspace
- *   of step 1, unchanged.
+ *   ubs_isect_sort_workspace_bytes(), its own buffer (step 2 reads nothing of
+ *   step 1's workspace; the counts it needs are isect_offsets).
  * Depths of visible primitives must be non-negative (the reference's key then
  * overflows into the tile field); a negative one makes step 1 fail. */
 size_t ubs_isect_count_workspace_bytes(int32_t C, int64_t N, int32_t n_tiles);

@@ -44,9 +44,16 @@ static uint32_t bit_width_u32(uint32_t v) {
 
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// Per-tile counters of the count pass in kCountReplicas replicas
+// ([replica][C * n_tiles], primitive entry idx counts in replica idx % R):
+// a tile's atomics spread over that many L2 lines; they are folded into
+// bucket_counts before the scan.
+constexpr int kCountReplicas = 8;
+
 struct CountWs {
     IsectHeader *hdr;
     int32_t *bucket_counts; // [C*n_tiles]
+    int32_t *replicas;      // [kCountReplicas][C*n_tiles]
     int64_t *block_sums;    // [n_scan_blocks]
     size_t bytes;
 };
@@ -59,6 +66,8 @@ static CountWs count_ws_layout(void *base, int32_t C, int64_t N, int32_t n_tiles
     w.hdr = reinterpret_cast<IsectHeader *>(p);
     w.bucket_counts = reinterpret_cast<int32_t *>(p + off);
     off = align256(off + nb * 4);
+    w.replicas = reinterpret_cast<int32_t *>(p + off);
+    off = align256(off + nb * kCountReplicas * 4);
     w.block_sums = reinterpret_cast<int64_t *>(p + off);
     off = align256(off + (nblocks + 1) * 8);
     w.bytes = off;
@@ -115,8 +124,8 @@ __device__ __forceinline__ Box tile_box(float mx, float my, int32_t radius, floa
 __global__ void isect_count_kernel(int64_t CN, int64_t N, const float2 *__restrict__ means2d,
                                    const int32_t *__restrict__ radii,
                                    const float *__restrict__ depths, float ts, uint32_t tw,
-                                   uint32_t th, int32_t *__restrict__ tiles_per_gauss,
-                                   int32_t *__restrict__ bucket_counts, uint32_t *status) {
+                                   uint32_t th, int64_t nb, int32_t *__restrict__ tiles_per_gauss,
+                                   int32_t *__restrict__ replicas, uint32_t *status) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= CN) return;
     const int32_t rad = radii[idx];
@@ -130,9 +139,19 @@ __global__ void isect_count_kernel(int64_t CN, int64_t N, const float2 *__restri
     if (b.x1 <= b.x0 || b.y1 <= b.y0) return;
     if (__float_as_int(depths[idx]) < 0) atomicOr(status, DEV_ERR_NEG_DEPTH);
     const int64_t cam = idx / N;
-    int32_t *bc = bucket_counts + cam * (int64_t)tw * th;
+    int32_t *bc = replicas + (idx % kCountReplicas) * nb + cam * (int64_t)tw * th;
     for (uint32_t y = b.y0; y < b.y1; ++y)
         for (uint32_t x = b.x0; x < b.x1; ++x) atomicAdd(&bc[y * tw + x], 1);
+}
+
+__global__ void fold_count_replicas_kernel(const int32_t *__restrict__ replicas, int64_t nb,
+                                           int32_t *__restrict__ counts) {
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    int32_t c = 0;
+#pragma unroll
+    for (int r = 0; r < kCountReplicas; ++r) c += replicas[r * nb + b];
+    counts[b] = c;
 }
 
 // ------------------------------------------------------------------- emit
@@ -261,16 +280,21 @@ int ubs_isect_count(int32_t C, int64_t N, const float *means2d, const int32_t *r
     const int64_t CN = (int64_t)C * N;
     const int64_t nb = (int64_t)C * n_tiles;
     if (cudaMemsetAsync(w.hdr, 0, sizeof(IsectHeader), st) != cudaSuccess ||
-        cudaMemsetAsync(w.bucket_counts, 0, nb * 4, st) != cudaSuccess)
+        cudaMemsetAsync(w.replicas, 0, nb * kCountReplicas * 4, st) != cudaSuccess)
         return check_launch("isect_count memset");
     if (CN > 0)
         UBS_TIMED("isect_count", st,
                   isect_count_kernel<<<grid_for(CN, 256), 256, 0, st>>>(
                       CN, N, reinterpret_cast<const float2 *>(means2d), radii, depths,
-                      (float)tile_size, (uint32_t)tile_width, (uint32_t)tile_height,
-                      tiles_per_gauss, w.bucket_counts, &w.hdr->status));
+                      (float)tile_size, (uint32_t)tile_width, (uint32_t)tile_height, nb,
+                      tiles_per_gauss, w.replicas, &w.hdr->status));
     ::ubs::note_launch();
     if (int e = check_launch("isect_count")) return e;
+    UBS_TIMED("isect_count_fold", st,
+              fold_count_replicas_kernel<<<grid_for(nb, 256), 256, 0, st>>>(w.replicas, nb,
+                                                                           w.bucket_counts));
+    ::ubs::note_launch();
+    if (int e = check_launch("isect_count fold")) return e;
     if (int e = device_exclusive_scan<int32_t>(w.bucket_counts, isect_offsets, nb, w.block_sums,
                                                &w.hdr->total, st))
         return e;
