@@ -389,11 +389,24 @@ template <int D> __global__ void __launch_bounds__(PRIM_THREADS) scene_prim_bwd_
     const int lane = threadIdx.x & 31;
     const int v = (int)(idx / a.N);
     const int64_t n = idx - (int64_t)v * a.N;
+    // the entry's own rows are requested before the warp stages the
+    // parameter rows, so both sets of loads are in flight together
+    const bool in = idx < (int64_t)a.C * a.N;
+    int32_t rad = 0;
+    float4 vr0 = make_float4(0.f, 0.f, 0.f, 0.f), vr1 = vr0, vr2 = vr0, c1 = vr0;
+    if (in) {
+        rad = a.radius[idx];
+        const float4 *vrow = reinterpret_cast<const float4 *>(a.v_rows + idx * kGradRow);
+        vr0 = vrow[0];
+        vr1 = vrow[1];
+        vr2 = vrow[2];
+        c1 = reinterpret_cast<const float4 *>(a.recs + idx)[1];
+    }
     PrimRows rows;
     if (prim_rows<D>(a, idx, n, lane, stage[threadIdx.x >> 5], rows)) __syncwarp();
-    if (idx >= (int64_t)a.C * a.N) return;
+    if (!in) return;
     const bool direct = a.C == 1; // one view: plain stores, else atomics into zeroed grads
-    if (a.radius[idx] <= 0) {
+    if (rad <= 0) {
         if (direct) {
 #pragma unroll
             for (int k = 0; k < 3; ++k) a.g_xyz[n * 3 + k] = 0.f;
@@ -411,14 +424,11 @@ template <int D> __global__ void __launch_bounds__(PRIM_THREADS) scene_prim_bwd_
         }
         return;
     }
-    const float4 *vrow = reinterpret_cast<const float4 *>(a.v_rows + idx * kGradRow);
-    const float4 vr0 = vrow[0], vr1 = vrow[1], vr2 = vrow[2];
     PrimFwd<D> f;
     prim_forward<D>(a, rows, v, f);
     const Cam cam = view_cam(a, v);
     const uint32_t W = (uint32_t)a.dims[v * 4], H = (uint32_t)a.dims[v * 4 + 1];
     // projection VJP (fully_fused_projection_bwd.cu:69-174) with the saved conic
-    const float4 c1 = reinterpret_cast<const float4 *>(a.recs + idx)[1];
     const float cn[3] = {c1.x, c1.y, c1.z};
     const float vcn[3] = {vr0.z, vr0.w, vr1.x};
     float vc2[4];
