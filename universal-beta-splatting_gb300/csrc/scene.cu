@@ -385,6 +385,7 @@ template <int D> __global__ void __launch_bounds__(PRIM_THREADS) scene_prim_bwd_
     constexpr int K = D - 3;
     constexpr int NL = D * (D - 1) / 2;
     __shared__ float stage[PRIM_THREADS / 32][stage_floats<D>()];
+    __shared__ float sraw[PRIM_THREADS / 32][32 * D]; // raw scale rows (softplus derivative)
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     const int v = (int)(idx / a.N);
@@ -403,7 +404,11 @@ template <int D> __global__ void __launch_bounds__(PRIM_THREADS) scene_prim_bwd_
         c1 = reinterpret_cast<const float4 *>(a.recs + idx)[1];
     }
     PrimRows rows;
-    if (prim_rows<D>(a, idx, n, lane, stage[threadIdx.x >> 5], rows)) __syncwarp();
+    const float *raw_s = a.scale + n * D;
+    if (prim_rows<D>(a, idx, n, lane, stage[threadIdx.x >> 5], rows)) {
+        raw_s = stage_rows<D>(a.scale, n - lane, sraw[threadIdx.x >> 5], lane);
+        __syncwarp();
+    }
     if (!in) return;
     const bool direct = a.C == 1; // one view: plain stores, else atomics into zeroed grads
     if (rad <= 0) {
@@ -507,7 +512,7 @@ template <int D> __global__ void __launch_bounds__(PRIM_THREADS) scene_prim_bwd_
 #pragma unroll
     for (int k = 0; k < K; ++k) put(&a.g_mean[n * K + k], gm[3 + k]);
 #pragma unroll
-    for (int k = 0; k < D; ++k) put(&a.g_scale[n * D + k], gs[k] * sigmoid_f(a.scale[n * D + k]));
+    for (int k = 0; k < D; ++k) put(&a.g_scale[n * D + k], gs[k] * sigmoid_f(raw_s[k]));
 #pragma unroll
     for (int k = 0; k < NL; ++k) put(&a.g_ltri[n * NL + k], gl[k]);
     put(&a.g_opac[n], go * f.o * (1.f - f.o));

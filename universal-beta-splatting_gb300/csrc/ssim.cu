@@ -380,9 +380,8 @@ __global__ void __launch_bounds__(L1_THREADS) l1_kernel(const float *__restrict_
                        reinterpret_cast<uintptr_t>(grad)) & 15) == 0;
     const int64_t stride = (int64_t)gridDim.x * L1_THREADS;
     if (vec) {
-        for (int64_t i = (int64_t)blockIdx.x * L1_THREADS + threadIdx.x; i < n4; i += stride) {
-            const float4 a = reinterpret_cast<const float4 *>(x)[i];
-            const float4 b = reinterpret_cast<const float4 *>(y)[i];
+        // two quads per step, both loads issued before either is used
+        auto quad = [&](const float4 &a, const float4 &b, int64_t i) {
             const float d0 = a.x - b.x, d1 = a.y - b.y, d2 = a.z - b.z, d3 = a.w - b.w;
             acc += fabsf(d0) + fabsf(d1) + fabsf(d2) + fabsf(d3);
             if (grad) {
@@ -390,6 +389,18 @@ __global__ void __launch_bounds__(L1_THREADS) l1_kernel(const float *__restrict_
                 reinterpret_cast<float4 *>(grad)[i] = make_float4(
                     gscale * sg(d0), gscale * sg(d1), gscale * sg(d2), gscale * sg(d3));
             }
+        };
+        for (int64_t i = (int64_t)blockIdx.x * L1_THREADS + threadIdx.x; i < n4; i += 2 * stride) {
+            const int64_t j = i + stride;
+            const float4 a = reinterpret_cast<const float4 *>(x)[i];
+            const float4 b = reinterpret_cast<const float4 *>(y)[i];
+            float4 a2 = make_float4(0.f, 0.f, 0.f, 0.f), b2 = a2;
+            if (j < n4) {
+                a2 = reinterpret_cast<const float4 *>(x)[j];
+                b2 = reinterpret_cast<const float4 *>(y)[j];
+            }
+            quad(a, b, i);
+            if (j < n4) quad(a2, b2, j);
         }
     }
     for (int64_t i = (vec ? n4 * 4 : 0) + (int64_t)blockIdx.x * L1_THREADS + threadIdx.x; i < n;
