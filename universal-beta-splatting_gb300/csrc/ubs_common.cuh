@@ -58,7 +58,8 @@ __device__ __forceinline__ float clamp01_eps(float x) {
 // ------------------------------------------ scene activation sections
 // Float offsets of the activated-parameter sections of the fused scene
 // workspace: scales [N, D] at 0, betas [N, D - 2] and opacities [N] each on a
-// 16-byte boundary (so that rows of 32 primitives can be bulk-copied).
+// 16-byte boundary, so that the activation pass writes every section with
+// 16-byte stores whatever N is.
 __host__ __device__ inline int64_t act_beta_off(int64_t N, int D) {
     return (N * D + 3) & ~int64_t(3);
 }
