@@ -533,30 +533,6 @@ __global__ void __launch_bounds__(256, 3) bucket_sort_warp_kernel(
     else warp_sort_bucket<32>(keys, lo, m, bkt, lane, w);
 }
 
-// Buckets of WARP_SEG < n <= SMALL_SEG keys (the mid list): a fixed grid walks
-// the device-side list; one CTA sorts a bucket in shared memory.
-template <typename Writer>
-__global__ void __launch_bounds__(SORT_THREADS) bucket_sort_mid_kernel(
-    int64_t n_buckets, const int32_t *__restrict__ offsets, const int64_t *T_dev, int64_t cap,
-    const uint64_t *__restrict__ keys, const int32_t *lists, const int32_t *counters, Writer w) {
-    __shared__ uint64_t s[SMALL_SEG];
-    const int n_mid = counters[1];
-    const int64_t T = T_dev ? imin64(*T_dev, cap) : cap;
-    for (int item = blockIdx.x; item < n_mid; item += gridDim.x) {
-        __syncthreads();
-        const int64_t bkt = lists[item];
-        int64_t lo, hi;
-        bucket_range(offsets, bkt, n_buckets, T, lo, hi);
-        const int n = (int)(hi - lo);
-        int n2 = 1;
-        while (n2 < n) n2 <<= 1;
-        for (int i = threadIdx.x; i < n2; i += blockDim.x) s[i] = i < n ? keys[lo + i] : ~0ull;
-        __syncthreads();
-        block_bitonic(s, n2);
-        for (int i = threadIdx.x; i < n; i += blockDim.x) w(s[i], lo + i, bkt);
-    }
-}
-
 // merge path: number of elements taken from a for output diagonal d
 __device__ __forceinline__ int64_t merge_split(const uint64_t *a, int64_t na, const uint64_t *b,
                                                int64_t nb, int64_t d) {
@@ -567,6 +543,72 @@ __device__ __forceinline__ int64_t merge_split(const uint64_t *a, int64_t na, co
         else hi = mid;
     }
     return lo;
+}
+
+// Buckets of WARP_SEG < n <= SMALL_SEG keys (the mid list): a fixed grid walks
+// the device-side list with one CTA of MID_WARPS warps per bucket.  Warp c
+// sorts keys [c WARP_SEG, (c + 1) WARP_SEG) in registers (warp_bitonic, 32 per
+// lane), the sorted runs are merged pairwise in shared memory by merge path,
+// and the last merge hands the sorted keys to the writer: two barriers per
+// merge level instead of one per bitonic stage (78 for 4096 keys).
+constexpr int MID_WARPS = SMALL_SEG / WARP_SEG;
+constexpr size_t MID_SMEM = 2 * SMALL_SEG * sizeof(uint64_t);
+template <typename Writer>
+__global__ void __launch_bounds__(MID_WARPS * 32, 3) bucket_sort_mid_kernel(
+    int64_t n_buckets, const int32_t *__restrict__ offsets, const int64_t *T_dev, int64_t cap,
+    const uint64_t *__restrict__ keys, const int32_t *lists, const int32_t *counters, Writer w) {
+    extern __shared__ __align__(16) uint64_t mid_runs[]; // two buffers of SMALL_SEG
+    const int n_mid = counters[1];
+    const int64_t T = T_dev ? imin64(*T_dev, cap) : cap;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int item = blockIdx.x; item < n_mid; item += gridDim.x) {
+        __syncthreads();
+        const int64_t bkt = lists[item];
+        int64_t lo, hi;
+        bucket_range(offsets, bkt, n_buckets, T, lo, hi);
+        const int n = (int)(hi - lo);
+        const int c0 = warp * WARP_SEG;
+        if (c0 < n) {
+            uint64_t v[32];
+#pragma unroll
+            for (int e = 0; e < 32; ++e) {
+                const int i = c0 + lane * 32 + e;
+                v[e] = i < n ? keys[lo + i] : ~0ull;
+            }
+            warp_bitonic<32>(v, lane);
+#pragma unroll
+            for (int e = 0; e < 32; ++e) { // the padding keys sort last: only real keys
+                const int i = c0 + lane * 32 + e;
+                if (i < n) mid_runs[i] = v[e];
+            }
+        }
+        __syncthreads();
+        uint64_t *src = mid_runs, *dst = mid_runs + SMALL_SEG;
+        for (int width = WARP_SEG; width < n; width <<= 1) {
+            const bool last = 2 * width >= n;
+            for (int r0 = 0; r0 < n; r0 += 2 * width) {
+                const int na = min(width, n - r0), nb = min(width, n - r0 - na);
+                const uint64_t *A = src + r0, *Bv = src + r0 + na;
+                const int total = na + nb;
+                for (int o0 = threadIdx.x * MERGE_ITEMS; o0 < total;
+                     o0 += blockDim.x * MERGE_ITEMS) {
+                    int ia = (int)merge_split(A, na, Bv, nb, o0);
+                    int ib = o0 - ia;
+                    const int oend = min(total, o0 + MERGE_ITEMS);
+                    for (int o = o0; o < oend; ++o) {
+                        const bool take_a = ib >= nb || (ia < na && A[ia] < Bv[ib]);
+                        const uint64_t key = take_a ? A[ia++] : Bv[ib++];
+                        if (last) w(key, lo + r0 + o, bkt);
+                        else dst[r0 + o] = key;
+                    }
+                }
+            }
+            __syncthreads();
+            uint64_t *t = src;
+            src = dst;
+            dst = t;
+        }
+    }
 }
 
 // Long buckets (their number is known only on the device): a fixed grid walks
@@ -638,8 +680,12 @@ inline int launch_bucket_sort(int64_t n_buckets, const int32_t *offsets, const i
     if (cap > WARP_SEG) {
         const int64_t max_mid = cap / (WARP_SEG + 1);
         const unsigned grid = (unsigned)imin64(imin64(max_mid, n_buckets), 152 * 6);
+        if (cudaFuncSetAttribute(bucket_sort_mid_kernel<Writer>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)MID_SMEM) != cudaSuccess)
+            return check_launch("bucket_sort_mid attribute");
         UBS_TIMED("bucket_sort_mid", st,
-                  bucket_sort_mid_kernel<Writer><<<grid, SORT_THREADS, 0, st>>>(
+                  bucket_sort_mid_kernel<Writer><<<grid, MID_WARPS * 32, MID_SMEM, st>>>(
                       n_buckets, offsets, T_dev, cap, keys, lists, counters, w));
         note_launch();
     }
