@@ -90,6 +90,10 @@ def parse():
                     help="with --profile: launch the step kernel by kernel instead of a graph")
     ap.add_argument("--dropin", action="store_true",
                     help="with --profile: the step through the drop-in gsplat operators")
+    ap.add_argument("--profile-config", choices=["C", "D"], default=None,
+                    help="run only the batched step of config C or D (tile 16, default blend "
+                         "variants: --warmup steps and one more) for an ncu capture; prints no "
+                         "JSON line")
     ap.add_argument("--profile-neighbours", action="store_true",
                     help="run each training-step neighbour (Adam, the losses, MCMC, scene "
                          "file, viewer frame) once on the 1M scene for an ncu capture; prints "
@@ -898,16 +902,40 @@ def run_config_a(dev, flush):
             "intersections": cs.n_isects}
 
 
+def config_views(name, dev):
+    """Parameters and cameras of config C (500k 7-D, 8 timestamped views
+    1352x1014) or D (3M 6-D, 4 views of mixed resolution)."""
+    from ubs import scene as S
+    if name == "C":
+        p = S.synthetic_params(500_000, 7, seed=0, xyz_range=2.0, device=dev)
+        rng = np.random.default_rng(0)
+        cams = [S.orbit_view(100 + i, 4.0, 1352, 1014, 1056.25, 1056.25,
+                             timestamp=float(rng.uniform()), device=dev) for i in range(8)]
+    else:
+        p = S.synthetic_params(3_000_000, 6, seed=0, xyz_range=2.0, device=dev)
+        res = [(1920, 1080), (1600, 1064), (1280, 720), (960, 540)]
+        cams = [S.orbit_view(200 + i, 4.0, w, h, 1500.0 * w / 1920, 1500.0 * w / 1920, device=dev)
+                for i, (w, h) in enumerate(res)]
+    for v in p.values():
+        v.requires_grad_(True)
+    return p, cams
+
+
+def profile_config(name, dev, warmup):
+    """The batched step of config C or D, warmup + 1 times, for an ncu capture."""
+    p, cams = config_views(name, dev)
+    st = TrainViews(p, cams, dev, TILE)
+    for _ in range(warmup + 1):
+        st.step()
+    torch.cuda.synchronize()
+    st.r._check_pending()
+    print("profile run: config %s" % name, flush=True)
+
+
 def run_config_c(dev, flush, rp):
     """500k 7-D dynamic primitives, 8 views of 1352x1014 with timestamps, one
     batched forward + backward."""
-    from ubs import scene as S
-    p = S.synthetic_params(500_000, 7, seed=0, xyz_range=2.0, device=dev)
-    for v in p.values():
-        v.requires_grad_(True)
-    rng = np.random.default_rng(0)
-    cams = [S.orbit_view(100 + i, 4.0, 1352, 1014, 1056.25, 1056.25,
-                         timestamp=float(rng.uniform()), device=dev) for i in range(8)]
+    p, cams = config_views("C", dev)
     ms, isects = _train_views(p, cams, dev, TILE, 10, flush)
     out = {"workload": "500k 7-D primitives, 8 views 1352x1014 (fx=fy=1056.25) with timestamps "
                        "U[0,1], one fused forward + L1 + backward", "ms_per_step": ms,
@@ -922,14 +950,8 @@ def run_config_c(dev, flush, rp):
 def run_config_d(dev, flush, rp):
     """3M 6-D primitives, 4 views of mixed resolution in one launch, tile size
     picked by the autotuner, peak memory reported."""
-    from ubs import scene as S
     from ubs.autotune import TileAutotuner
-    p = S.synthetic_params(3_000_000, 6, seed=0, xyz_range=2.0, device=dev)
-    for v in p.values():
-        v.requires_grad_(True)
-    res = [(1920, 1080), (1600, 1064), (1280, 720), (960, 540)]
-    cams = [S.orbit_view(200 + i, 4.0, w, h, 1500.0 * w / 1920, 1500.0 * w / 1920, device=dev)
-            for i, (w, h) in enumerate(res)]
+    p, cams = config_views("D", dev)
     tuner = TileAutotuner(reps=3)
     states = {}
 
@@ -1309,6 +1331,9 @@ def main():
     torch.cuda.set_device(dev)
     from ubs import _lib as L
     L.lib()
+    if args.profile_config:
+        profile_config(args.profile_config, dev, args.warmup)
+        return
     p, cam, ri, rj, bg, target = make_problem(args.n_prims, rank, dev)
     fz = FusedStep(p, cam, bg, target, dev)
     if args.profile_neighbours:
